@@ -1,0 +1,327 @@
+"""ctypes wrapper over the CPU oracle (oracle/flyoracle.cpp).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the CPU legs of bench.py as
+the checker. The product package never imports this module.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_SO = os.path.join(_HERE, "_build", "libflyoracle.so")
+
+OK, INVALID, SPLINE_OOB, GHOST_OVERFLOW = 0, 1, 2, 3
+
+
+class OracleError(RuntimeError):
+    def __init__(self, status: int, what: str):
+        super().__init__(f"oracle {what} failed with status {status}")
+        self.status = status
+
+
+def build() -> str:
+    """Compile the oracle with its Makefile (a few seconds)."""
+    subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    return _SO
+
+
+class DimerOptions(C.Structure):
+    """Dimer::Options (dimer.hpp:56-98) followed by Rotor::Options (rotor.hpp:47-60)."""
+
+    _fields_ = [
+        ("n", C.c_int), ("max_steps", C.c_int), ("hist_check_freq", C.c_int), ("use_history", C.c_int),
+        ("f2norm", C.c_double), ("skin_frac", C.c_double), ("proj_tol", C.c_double), ("max_trust", C.c_double),
+        ("min_trust", C.c_double), ("grow_trust", C.c_double), ("shrink_trust", C.c_double),
+        ("convex_max", C.c_double),
+        ("rot_n", C.c_int), ("iter_max_rot", C.c_int), ("relax_in_convex", C.c_int), ("pad_", C.c_int),
+        ("delta_r", C.c_double), ("theta_tol", C.c_double),
+    ]
+
+    @classmethod
+    def defaults(cls, **kw) -> "DimerOptions":
+        o = cls(n=10, max_steps=1000, hist_check_freq=5, use_history=1, f2norm=1e-5, skin_frac=1.1, proj_tol=0.0,
+                max_trust=0.5, min_trust=0.05, grow_trust=1.5, shrink_trust=0.5, convex_max=3.0, rot_n=6,
+                iter_max_rot=20, relax_in_convex=1, pad_=0, delta_r=0.001, theta_tol=np.pi / 360.0)
+        for k, v in kw.items():
+            setattr(o, k, v)
+        return o
+
+
+class LBFGSOptions(C.Structure):
+    """LBFGS::Options (lbfgs.hpp:56-80)."""
+
+    _fields_ = [
+        ("n", C.c_int), ("iter_max", C.c_int), ("f2norm", C.c_double), ("skin_frac", C.c_double),
+        ("proj_tol", C.c_double), ("max_trust", C.c_double), ("min_trust", C.c_double),
+        ("grow_trust", C.c_double), ("shrink_trust", C.c_double),
+    ]
+
+    @classmethod
+    def defaults(cls, **kw) -> "LBFGSOptions":
+        o = cls(n=10, iter_max=2000, f2norm=1e-6, skin_frac=1.1, proj_tol=0.0, max_trust=0.5, min_trust=0.01,
+                grow_trust=1.5, shrink_trust=0.5)
+        for k, v in kw.items():
+            setattr(o, k, v)
+        return o
+
+
+_dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+_ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+_lp = np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS")
+_up = np.ctypeslib.ndpointer(dtype=np.uint32, flags="C_CONTIGUOUS")
+_bp = np.ctypeslib.ndpointer(dtype=np.uint8, flags="C_CONTIGUOUS")
+_u64p = np.ctypeslib.ndpointer(dtype=np.uint64, flags="C_CONTIGUOUS")
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        if not os.path.exists(_SO):
+            build()
+        L = C.CDLL(_SO)
+        V = C.c_void_p
+        L.orc_eam_load.restype = V
+        L.orc_eam_load.argtypes = [C.c_char_p]
+        L.orc_eam_free.argtypes = [V]
+        L.orc_eam_rcut.restype = C.c_double
+        L.orc_eam_rcut.argtypes = [V]
+        L.orc_eam_ntypes.argtypes = [V]
+        L.orc_eam_mass.restype = C.c_double
+        L.orc_eam_mass.argtypes = [V, C.c_int]
+        L.orc_spline_eval.argtypes = [V, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.POINTER(C.c_double)]
+        L.orc_spline_table.restype = C.c_long
+        L.orc_spline_table.argtypes = [V, C.c_int, C.c_int, C.c_int, V, C.c_long]
+        L.orc_list_new.restype = V
+        L.orc_list_new.argtypes = [_dp, _ip, C.c_double]
+        L.orc_list_free.argtypes = [V]
+        L.orc_list_rebuild.argtypes = [V, _dp, C.c_long, C.c_int]
+        L.orc_list_update.argtypes = [V, _dp]
+        L.orc_list_num_ghosts.restype = C.c_long
+        L.orc_list_num_ghosts.argtypes = [V]
+        L.orc_list_shape.argtypes = [V, _ip]
+        L.orc_list_slots.restype = C.c_long
+        L.orc_list_slots.argtypes = [V, V, V, C.c_long]
+        L.orc_list_neighbours.restype = C.c_long
+        L.orc_list_neighbours.argtypes = [V, C.c_double, _ip, V, V, C.c_long]
+        L.orc_list_raw.restype = C.c_long
+        L.orc_list_raw.argtypes = [V, _ip, V, C.c_long]
+        L.orc_eam_energy.argtypes = [V, V, _up, C.c_int, C.POINTER(C.c_double)]
+        L.orc_eam_gradient.argtypes = [V, V, _up, _bp, C.c_int, _dp]
+        L.orc_eam_fprime.argtypes = [V, V, _up, _bp, _dp]
+        L.orc_brute_neighbours.restype = C.c_long
+        L.orc_brute_neighbours.argtypes = [_dp, _ip, _dp, C.c_long, C.c_double, _ip, V, V, C.c_long]
+        L.orc_lbfgs_minimise.argtypes = [V, C.POINTER(LBFGSOptions), _dp, _ip, C.c_long, _dp, _up, _bp, _dp,
+                                         C.POINTER(C.c_int), C.POINTER(C.c_int)]
+        L.orc_dimer_find_sp.argtypes = [V, C.POINTER(DimerOptions), _dp, _ip, C.c_long, _dp, _dp, _up, _bp, _dp, V,
+                                        C.c_int, C.c_double, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                        C.POINTER(C.c_long), C.POINTER(C.c_double)]
+        L.orc_dimer_batch.argtypes = [V, C.POINTER(DimerOptions), C.c_int, _lp, _dp, _ip, _dp, _dp, _up, _bp, _ip,
+                                      C.c_int, _ip, _ip]
+        L.orc_xoshiro.argtypes = [_u64p, _u64p, C.c_long]
+        L.orc_max_threads.restype = C.c_int
+        _lib = L
+    return _lib
+
+
+def _check(st: int, what: str) -> None:
+    if st != OK:
+        raise OracleError(st, what)
+
+
+def xoshiro(seed, n: int) -> np.ndarray:
+    out = np.zeros(n, dtype=np.uint64)
+    lib().orc_xoshiro(np.asarray(seed, dtype=np.uint64), out, n)
+    return out
+
+
+class EAMData:
+    """DataEAM (data.cpp:67-153) parsed by the oracle."""
+
+    def __init__(self, path: str):
+        self.h = lib().orc_eam_load(path.encode())
+        if not self.h:
+            raise OracleError(INVALID, f"load {path}")
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_eam_free(self.h)
+            self.h = None
+
+    @property
+    def r_cut(self) -> float:
+        return lib().orc_eam_rcut(self.h)
+
+    @property
+    def n_types(self) -> int:
+        return lib().orc_eam_ntypes(self.h)
+
+    def mass(self, t: int) -> float:
+        return lib().orc_eam_mass(self.h, t)
+
+    def spline(self, kind: int, a: int, b: int, deriv: int, x: float) -> float:
+        out = C.c_double()
+        _check(lib().orc_spline_eval(self.h, kind, a, b, deriv, x, C.byref(out)), "spline")
+        return out.value
+
+    def table(self, kind: int, a: int, b: int = 0) -> np.ndarray:
+        n = lib().orc_spline_table(self.h, kind, a, b, None, 0)
+        out = np.zeros((n, 4), dtype=np.float64)
+        lib().orc_spline_table(self.h, kind, a, b, out.ctypes.data, out.size)
+        return out
+
+
+class List:
+    """neigh::List (list.hpp:71-211) restated."""
+
+    def __init__(self, extents, periodic, r_cut: float):
+        self.ext = np.ascontiguousarray(extents, dtype=np.float64)
+        self.per = np.ascontiguousarray(periodic, dtype=np.int32)
+        self.h = lib().orc_list_new(self.ext, self.per, float(r_cut))
+        if not self.h:
+            raise OracleError(INVALID, "List()")
+        self.n = 0
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_list_free(self.h)
+            self.h = None
+
+    def rebuild(self, pos: np.ndarray, threads: int = 1) -> None:
+        pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1)
+        self.n = pos.size // 3
+        _check(lib().orc_list_rebuild(self.h, pos, self.n, threads), "rebuild")
+
+    def update(self, delta: np.ndarray) -> None:
+        _check(lib().orc_list_update(self.h, np.ascontiguousarray(delta, dtype=np.float64).reshape(-1)), "update")
+
+    @property
+    def num_ghosts(self) -> int:
+        return lib().orc_list_num_ghosts(self.h)
+
+    def shape(self) -> np.ndarray:
+        s = np.zeros(3, dtype=np.int32)
+        lib().orc_list_shape(self.h, s)
+        return s
+
+    def slots(self):
+        tot = lib().orc_list_slots(self.h, None, None, 0)
+        pos = np.zeros((tot, 3), dtype=np.float64)
+        img = np.zeros(tot, dtype=np.int64)
+        lib().orc_list_slots(self.h, pos.ctypes.data, img.ctypes.data, tot)
+        return pos, img
+
+    def neighbours(self, r_cut: float):
+        """(counts, real indices, dr) in for_neighbours order, CSR."""
+        counts = np.zeros(self.n, dtype=np.int32)
+        tot = lib().orc_list_neighbours(self.h, r_cut, counts, None, None, 0)
+        if tot < 0:
+            raise OracleError(INVALID, "neighbours")
+        idx = np.zeros(tot, dtype=np.int32)
+        dr = np.zeros((tot, 3), dtype=np.float64)
+        lib().orc_list_neighbours(self.h, r_cut, counts, idx.ctypes.data, dr.ctypes.data, tot)
+        return counts, idx, dr
+
+    def raw(self):
+        counts = np.zeros(self.n, dtype=np.int32)
+        tot = lib().orc_list_raw(self.h, counts, None, 0)
+        slots = np.zeros(tot, dtype=np.int32)
+        lib().orc_list_raw(self.h, counts, slots.ctypes.data, tot)
+        return counts, slots
+
+
+def eam_energy(data: EAMData, nl: List, types: np.ndarray, threads: int = 1) -> float:
+    e = C.c_double()
+    _check(lib().orc_eam_energy(data.h, nl.h, np.ascontiguousarray(types, dtype=np.uint32), threads, C.byref(e)),
+           "energy")
+    return e.value
+
+
+def eam_gradient(data: EAMData, nl: List, types: np.ndarray, frozen: np.ndarray, threads: int = 1) -> np.ndarray:
+    g = np.zeros(3 * nl.n, dtype=np.float64)
+    _check(lib().orc_eam_gradient(data.h, nl.h, np.ascontiguousarray(types, dtype=np.uint32),
+                                  np.ascontiguousarray(frozen, dtype=np.uint8), threads, g), "gradient")
+    return g.reshape(-1, 3)
+
+
+def eam_fprime(data: EAMData, nl: List, types: np.ndarray, frozen: np.ndarray) -> np.ndarray:
+    fp = np.zeros(nl.n, dtype=np.float64)
+    _check(lib().orc_eam_fprime(data.h, nl.h, np.ascontiguousarray(types, dtype=np.uint32),
+                                np.ascontiguousarray(frozen, dtype=np.uint8), fp), "fprime")
+    return fp
+
+
+def brute_neighbours(extents, periodic, pos: np.ndarray, r_cut: float):
+    ext = np.ascontiguousarray(extents, dtype=np.float64)
+    per = np.ascontiguousarray(periodic, dtype=np.int32)
+    pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1)
+    n = pos.size // 3
+    counts = np.zeros(n, dtype=np.int32)
+    tot = lib().orc_brute_neighbours(ext, per, pos, n, r_cut, counts, None, None, 0)
+    idx = np.zeros(tot, dtype=np.int32)
+    dr = np.zeros((tot, 3), dtype=np.float64)
+    lib().orc_brute_neighbours(ext, per, pos, n, r_cut, counts, idx.ctypes.data, dr.ctypes.data, tot)
+    return counts, idx, dr
+
+
+def lbfgs_minimise(data: EAMData, opt: LBFGSOptions, extents, periodic, pos, types, frozen):
+    """Returns (failed, iters, positions, gradient)."""
+    x = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1).copy()
+    g = np.zeros_like(x)
+    failed, iters = C.c_int(), C.c_int()
+    _check(lib().orc_lbfgs_minimise(data.h, C.byref(opt), np.ascontiguousarray(extents, dtype=np.float64),
+                                    np.ascontiguousarray(periodic, dtype=np.int32), x.size // 3, x,
+                                    np.ascontiguousarray(types, dtype=np.uint32),
+                                    np.ascontiguousarray(frozen, dtype=np.uint8), g, C.byref(failed),
+                                    C.byref(iters)), "lbfgs")
+    return bool(failed.value), iters.value, x.reshape(-1, 3), g.reshape(-1, 3)
+
+
+def dimer_find_sp(data: EAMData, opt: DimerOptions, extents, periodic, pos, axis, types, frozen, in_min=None,
+                  hist=None, theta_tol: float = 0.0, count_frozen: int | None = None):
+    """Dimer::find_sp. Returns dict(exit, steps, grad_calls, curv, x, axis)."""
+    x = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1).copy()
+    ax = np.ascontiguousarray(axis, dtype=np.float64).reshape(-1).copy()
+    fz = np.ascontiguousarray(frozen, dtype=np.uint8)
+    if count_frozen is None:
+        count_frozen = int(fz.sum())
+    im = x.copy() if in_min is None else np.ascontiguousarray(in_min, dtype=np.float64).reshape(-1)
+    n_hist = 0
+    hp = None
+    if hist is not None and len(hist):
+        h = np.ascontiguousarray(np.stack([np.asarray(s, dtype=np.float64).reshape(-1) for s in hist]))
+        n_hist, hp = h.shape[0], h
+    ex, st, gc, cv = C.c_int(), C.c_int(), C.c_long(), C.c_double()
+    _check(lib().orc_dimer_find_sp(data.h, C.byref(opt), np.ascontiguousarray(extents, dtype=np.float64),
+                                   np.ascontiguousarray(periodic, dtype=np.int32), x.size // 3, x, ax,
+                                   np.ascontiguousarray(types, dtype=np.uint32), fz, im,
+                                   None if hp is None else hp.ctypes.data, n_hist, theta_tol, count_frozen,
+                                   C.byref(ex), C.byref(st), C.byref(gc), C.byref(cv)), "dimer")
+    return dict(exit=ex.value, steps=st.value, grad_calls=gc.value, curv=cv.value, x=x.reshape(-1, 3),
+                axis=ax.reshape(-1, 3))
+
+
+def dimer_batch(data: EAMData, opt: DimerOptions, offsets, extents, periodic, pos, axis, types, frozen,
+                count_frozen, threads: int):
+    """Independent searches spread over threads (Master::find_batch's fan-out). In-place on copies."""
+    x = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1).copy()
+    ax = np.ascontiguousarray(axis, dtype=np.float64).reshape(-1).copy()
+    ns = len(offsets) - 1
+    ex = np.zeros(ns, dtype=np.int32)
+    st = np.zeros(ns, dtype=np.int32)
+    _check(lib().orc_dimer_batch(data.h, C.byref(opt), ns, np.ascontiguousarray(offsets, dtype=np.int64),
+                                 np.ascontiguousarray(extents, dtype=np.float64).reshape(-1),
+                                 np.ascontiguousarray(periodic, dtype=np.int32).reshape(-1), x, ax,
+                                 np.ascontiguousarray(types, dtype=np.uint32),
+                                 np.ascontiguousarray(frozen, dtype=np.uint8),
+                                 np.ascontiguousarray(count_frozen, dtype=np.int32), threads, ex, st), "dimer_batch")
+    return ex, st, x.reshape(-1, 3), ax.reshape(-1, 3)
+
+
+def max_threads() -> int:
+    return lib().orc_max_threads()
