@@ -1,0 +1,112 @@
+/* flygpu.h -- C ABI of the GB300 (sm_103a) saddle-search inner loop.
+ *
+ * The reference (openFLY) runs this path in C++ behind three interfaces:
+ *   fly::neigh::List            include/libfly/neigh/list.hpp:71-211
+ *   fly::potential::EAM/Generic include/libfly/potential/EAM/eam.hpp:42-120, potential/generic.hpp:50-140
+ *   fly::saddle::Dimer / fly::minimise::LBFGS
+ *                               include/libfly/saddle/dimer.hpp:51-170, minimise/LBFGS/lbfgs.hpp:48-128
+ * Each entry point below names the reference member it replaces. Conventions:
+ *   - every function returns an int status (FLYGPU_OK = 0); flygpu_last_error() gives detail;
+ *   - host arrays use the reference's layout: positions, axes, deltas and gradients are interleaved
+ *     xyz doubles, 3 per atom (system/adaptor.hpp:77); types are uint32 (TypeID, property.hpp:113);
+ *     frozen flags are one byte per atom (Frozen, property.hpp:192);
+ *   - "_device" variants take device pointers of the same layout and do not synchronise;
+ *   - handles are not thread-safe: use one per host thread (the reference keeps one potential and one
+ *     List per OpenMP thread, saddle/find.hpp:310-317). The server handle is internally synchronised.
+ */
+#ifndef FLYGPU_H
+#define FLYGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum flygpu_status_code {
+  FLYGPU_OK = 0,
+  FLYGPU_INVALID_ARG = 1,     /* fly::RuntimeError from verify() (utility/core.hpp:89-137) */
+  FLYGPU_SPLINE_OOB = 2,      /* Spline::OutOfBounds (utility/spline.hpp:46-51,141-143) */
+  FLYGPU_GHOST_OVERFLOW = 3,  /* more than List::MAX_GHOST_RATIO * n ghosts (neigh/list.hpp:78) */
+  FLYGPU_NLIST_OVERFLOW = 4,  /* neighbour capacity exceeded after one automatic regrow */
+  FLYGPU_OOM = 5,             /* device or pinned allocation failed */
+  FLYGPU_TIMEOUT = 6,         /* a search hit its device-side iteration budget */
+  FLYGPU_CUDA_ERROR = 7       /* any other CUDA runtime error */
+};
+
+/* Arithmetic of the EAM passes. FP64: every operation in binary64 without contraction, the
+ * reference's arithmetic. MIXED: spline lookups and pair terms in binary32, per-atom density,
+ * energy and force accumulators in binary64. */
+enum flygpu_precision { FLYGPU_FP64 = 0, FLYGPU_MIXED = 1 };
+
+/* Dimer::Exit (saddle/dimer.hpp:123-129) */
+enum flygpu_exit { FLYGPU_EXIT_SUCCESS = 0, FLYGPU_EXIT_CONVEX = -1, FLYGPU_EXIT_ITER_MAX = -2,
+                   FLYGPU_EXIT_COLLISION = -3, FLYGPU_EXIT_UNINIT = -4 };
+
+typedef struct flygpu_eam flygpu_eam;
+typedef struct flygpu_list flygpu_list;
+typedef struct flygpu_server flygpu_server;
+
+const char* flygpu_status_string(int status);
+/* Message of the last failing call on this host thread ("" if none). */
+const char* flygpu_last_error(void);
+
+/* ---------------------------------------------------------------- EAM tables
+ * Replaces DataEAM::DataEAM (potential/EAM/data.hpp:54, src/potential/EAM/data.cpp:67-153): parses a
+ * LAMMPS eam/fs file, builds the natural cubic splines (utility/spline.hpp:66, spline.cpp:27-103)
+ * on the host and uploads binary64 and binary32 coefficient tables. */
+int flygpu_eam_load(const char* path, flygpu_eam** out);
+void flygpu_eam_destroy(flygpu_eam* eam);
+/* EAM::r_cut (potential/EAM/eam.hpp:71) */
+double flygpu_eam_r_cut(const flygpu_eam* eam);
+int flygpu_eam_n_types(const flygpu_eam* eam);
+/* Host copy of one function's binary64 coefficients {a,b,c,d} per interval: kind 0 = F(type a),
+ * 1 = phi(a, b), 2 = v(a, b). Returns the interval count; copies if cap >= 4 * count. */
+int64_t flygpu_eam_table(const flygpu_eam* eam, int kind, int a, int b, double* out, int64_t cap);
+
+/* ---------------------------------------------------------------- neighbour list
+ * Replaces neigh::List::List(box, r_cut) (neigh/list.hpp:86-90) for an orthorhombic box
+ * (system/boxes/orthorhombic.hpp:115-118). stream may be NULL (the handle then owns one). */
+int flygpu_list_create(const double extents[3], const int periodic[3], double r_cut, void* stream,
+                       flygpu_list** out);
+void flygpu_list_destroy(flygpu_list* list);
+/* List::rebuild (neigh/list.hpp:98, src/neigh/list.cpp:53-95). pos: 3n doubles. */
+int flygpu_list_rebuild(flygpu_list* list, const double* pos, int64_t n);
+int flygpu_list_rebuild_device(flygpu_list* list, const double* d_pos, int64_t n);
+/* List::update (neigh/list.hpp:118, src/neigh/list.cpp:37-51): r <- r - delta for real and ghost
+ * atoms. delta: 3n doubles. */
+int flygpu_list_update(flygpu_list* list, const double* delta);
+int flygpu_list_update_device(flygpu_list* list, const double* d_delta);
+/* List::size (neigh/list.hpp:161) */
+int64_t flygpu_list_size(const flygpu_list* list);
+int64_t flygpu_list_num_ghosts(const flygpu_list* list);
+/* Every (atom, neighbour) pair that List::for_neighbours (neigh/list.hpp:139-154) visits within
+ * r_cut, in its visiting order: counts[n] per atom, then CSR real indices idx[] and dr[3*] (neighbour
+ * minus atom). total receives the pair count; idx/dr are filled when cap >= total. */
+int flygpu_list_neighbours(flygpu_list* list, double r_cut, int32_t* counts, int32_t* idx, double* dr,
+                           int64_t cap, int64_t* total);
+/* Wait for the list's stream and report the first device-side error raised since the last call. */
+int flygpu_list_sync(flygpu_list* list);
+
+/* ---------------------------------------------------------------- EAM energy / gradient
+ * types (n uint32) and frozen (n bytes) are uploaded when non-NULL and reused when NULL. */
+/* EAM::energy (potential/EAM/eam.hpp:83, src/potential/EAM/eam.cpp:33-51) */
+int flygpu_eam_energy(flygpu_eam* eam, flygpu_list* list, const uint32_t* types, const uint8_t* frozen,
+                      int precision, double* energy);
+/* EAM::gradient (potential/EAM/eam.hpp:95, src/potential/EAM/eam.cpp:53-120). grad: 3n doubles. */
+int flygpu_eam_gradient(flygpu_eam* eam, flygpu_list* list, const uint32_t* types, const uint8_t* frozen,
+                        int precision, double* grad);
+/* Both in one density pass + one force pass (energy may be NULL). */
+int flygpu_eam_energy_gradient(flygpu_eam* eam, flygpu_list* list, const uint32_t* types,
+                               const uint8_t* frozen, int precision, double* energy, double* grad);
+/* Device-pointer form of the above: d_types / d_frozen may be NULL (reuse), d_energy may be NULL. */
+int flygpu_eam_energy_gradient_device(flygpu_eam* eam, flygpu_list* list, const uint32_t* d_types,
+                                      const uint8_t* d_frozen, int precision, double* d_energy,
+                                      double* d_grad);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FLYGPU_H */

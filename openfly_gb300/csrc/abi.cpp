@@ -1,0 +1,266 @@
+// abi.cpp -- extern "C" entry points of libflygpu (declared in include/flygpu.h).
+
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <new>
+
+#include "internal.hpp"
+
+namespace flygpu {
+
+  namespace {
+    thread_local std::string g_last_error;
+  }
+
+  void set_error(std::string msg) { g_last_error = std::move(msg); }
+
+  void fail(int status, std::string msg) { throw Error{status, std::move(msg)}; }
+
+  int status_from_word(int w) {
+    if (w & ERR_GHOST_OVERFLOW) return FLYGPU_GHOST_OVERFLOW;
+    if (w & ERR_NLIST_OVERFLOW) return FLYGPU_NLIST_OVERFLOW;
+    if (w & ERR_SPLINE_OOB) return FLYGPU_SPLINE_OOB;
+    if (w & ERR_TIMEOUT) return FLYGPU_TIMEOUT;
+    if (w & ERR_BAD_INDEX) return FLYGPU_INVALID_ARG;
+    return FLYGPU_OK;
+  }
+
+  flygpu_eam* eam_load(char const* path);
+
+  // Runs f, converting exceptions into a status and recording the message.
+  template <typename F>
+  int guard(F&& f) {
+    try {
+      f();
+      return FLYGPU_OK;
+    } catch (Error const& e) {
+      set_error(e.msg);
+      return e.status;
+    } catch (std::bad_alloc const&) {
+      set_error("host allocation failed");
+      return FLYGPU_OOM;
+    } catch (std::exception const& e) {
+      set_error(e.what());
+      return FLYGPU_INVALID_ARG;
+    }
+  }
+
+  // Syncs the list's stream and converts its device error word into a status.
+  void check_device(flygpu_list* L) {
+    int const w = list_take_error(L);
+    if (w) {
+      int const st = status_from_word(w);
+      fail(st, st == FLYGPU_SPLINE_OOB ? "spline argument outside the tabulated region"
+                                       : "device-side error word " + std::to_string(w));
+    }
+  }
+
+  void need(bool ok, char const* what) {
+    if (!ok) fail(FLYGPU_INVALID_ARG, what);
+  }
+
+  void run_eam(flygpu_eam* E, flygpu_list* L, int precision, double* d_energy, double* d_grad) {
+    need(E && L, "null handle");
+    need(precision == FLYGPU_FP64 || precision == FLYGPU_MIXED, "unknown precision");
+    if (precision == FLYGPU_FP64) {
+      eam_fp64(E, L, d_energy, d_grad);
+    } else {
+      eam_mixed(E, L, d_energy, d_grad);
+    }
+  }
+
+}  // namespace flygpu
+
+using namespace flygpu;
+
+extern "C" {
+
+const char* flygpu_status_string(int status) {
+  switch (status) {
+    case FLYGPU_OK: return "ok";
+    case FLYGPU_INVALID_ARG: return "invalid argument";
+    case FLYGPU_SPLINE_OOB: return "spline out of bounds";
+    case FLYGPU_GHOST_OVERFLOW: return "ghost capacity exceeded";
+    case FLYGPU_NLIST_OVERFLOW: return "neighbour capacity exceeded";
+    case FLYGPU_OOM: return "out of memory";
+    case FLYGPU_TIMEOUT: return "device iteration budget exhausted";
+    case FLYGPU_CUDA_ERROR: return "CUDA error";
+    default: return "unknown status";
+  }
+}
+
+const char* flygpu_last_error(void) { return g_last_error.c_str(); }
+
+int flygpu_eam_load(const char* path, flygpu_eam** out) {
+  return guard([&] {
+    need(path && out, "null argument");
+    *out = nullptr;
+    *out = eam_load(path);
+  });
+}
+
+void flygpu_eam_destroy(flygpu_eam* eam) { delete eam; }
+
+double flygpu_eam_r_cut(const flygpu_eam* eam) { return eam ? eam->r_cut : 0.0; }
+
+int flygpu_eam_n_types(const flygpu_eam* eam) { return eam ? eam->n_types : 0; }
+
+int64_t flygpu_eam_table(const flygpu_eam* eam, int kind, int a, int b, double* out, int64_t cap) {
+  if (!eam || kind < 0 || kind > 2 || a < 0 || a >= eam->n_types || b < 0 || b >= eam->n_types) return -1;
+  SplineSet const& s = kind == 0 ? eam->F : kind == 1 ? eam->phi : eam->v;
+  int const fn = kind == 0 ? a : a + eam->n_types * b;
+  int64_t const count = s.n_spines;
+  if (out && cap >= 4 * count)
+    std::memcpy(out, &s.host[static_cast<std::size_t>(fn) * static_cast<std::size_t>(count) * 4],
+                sizeof(double) * static_cast<std::size_t>(4 * count));
+  return count;
+}
+
+int flygpu_list_create(const double extents[3], const int periodic[3], double r_cut, void* stream, flygpu_list** out) {
+  return guard([&] {
+    need(extents && periodic && out, "null argument");
+    *out = nullptr;
+    need(r_cut > 0, "r_cut must be positive");
+    auto L = std::make_unique<flygpu_list>();
+    GridDesc& g = L->g;
+    g.rc = r_cut;
+    for (int k = 0; k < 3; ++k) {
+      need(extents[k] > 0, "box extents must be positive");
+      need(extents[k] > r_cut, "r_cut is too big for the box");  // hypergrid.hpp:46-48
+      g.L[k] = extents[k];
+      g.per[k] = periodic[k] ? 1 : 0;
+      g.shape[k] = 2 + static_cast<int>(extents[k] / r_cut);
+      g.cell[k] = extents[k] / std::floor(extents[k] / r_cut);
+      g.inv_cell[k] = 1.0 / g.cell[k];
+      double const C = std::exp2(std::ceil(std::log2(extents[k] + 4 * r_cut + 1)));
+      L->shift[k] = C + 2 * r_cut;
+    }
+    need(static_cast<double>(g.shape[0]) * g.shape[1] * g.shape[2] < 2e9, "too many cells");
+    if (stream) {
+      L->stream = static_cast<cudaStream_t>(stream);
+    } else {
+      FLY_CUDA(cudaStreamCreateWithFlags(&L->stream, cudaStreamNonBlocking));
+      L->own_stream = true;
+    }
+    L->err.reserve(1);
+    L->counters.reserve(8);
+    L->h_small.reserve(8);
+    FLY_CUDA(cudaMemsetAsync(L->err.p, 0, sizeof(int), L->stream));
+    FLY_CUDA(cudaStreamSynchronize(L->stream));
+    *out = L.release();
+  });
+}
+
+void flygpu_list_destroy(flygpu_list* list) {
+  if (!list) return;
+  if (list->stream) cudaStreamSynchronize(list->stream);
+  bool const own = list->own_stream;
+  cudaStream_t const s = list->stream;
+  delete list;
+  if (own) cudaStreamDestroy(s);
+}
+
+int flygpu_list_rebuild(flygpu_list* list, const double* pos, int64_t n) {
+  return guard([&] {
+    need(list && (pos || n == 0), "null argument");
+    need(n >= 0, "negative atom count");
+    list->io.reserve(static_cast<std::size_t>(3 * n + 3));
+    if (n) FLY_CUDA(cudaMemcpyAsync(list->io.p, pos, sizeof(double) * 3 * static_cast<std::size_t>(n),
+                                    cudaMemcpyHostToDevice, list->stream));
+    list_rebuild(list, list->io.p, n);
+    check_device(list);
+  });
+}
+
+int flygpu_list_rebuild_device(flygpu_list* list, const double* d_pos, int64_t n) {
+  return guard([&] {
+    need(list && (d_pos || n == 0), "null argument");
+    list_rebuild(list, d_pos, n);
+  });
+}
+
+int flygpu_list_update(flygpu_list* list, const double* delta) {
+  return guard([&] {
+    need(list && delta, "null argument");
+    std::size_t const n3 = 3 * static_cast<std::size_t>(list->n);
+    list->io.reserve(n3 + 3);
+    if (n3) FLY_CUDA(cudaMemcpyAsync(list->io.p, delta, sizeof(double) * n3, cudaMemcpyHostToDevice, list->stream));
+    list_update(list, list->io.p);
+  });
+}
+
+int flygpu_list_update_device(flygpu_list* list, const double* d_delta) {
+  return guard([&] {
+    need(list && d_delta, "null argument");
+    list_update(list, d_delta);
+  });
+}
+
+int64_t flygpu_list_size(const flygpu_list* list) { return list ? list->n : 0; }
+
+int64_t flygpu_list_num_ghosts(const flygpu_list* list) { return list ? list->n_slots - list->n : 0; }
+
+int flygpu_list_neighbours(flygpu_list* list, double r_cut, int32_t* counts, int32_t* idx, double* dr, int64_t cap,
+                           int64_t* total) {
+  return guard([&] {
+    need(list && total, "null argument");
+    *total = list_export(list, r_cut, counts, idx, dr, cap);
+    check_device(list);
+  });
+}
+
+int flygpu_list_sync(flygpu_list* list) {
+  return guard([&] {
+    need(list, "null handle");
+    FLY_CUDA(cudaStreamSynchronize(list->stream));
+    check_device(list);
+  });
+}
+
+int flygpu_eam_energy_gradient(flygpu_eam* eam, flygpu_list* list, const uint32_t* types, const uint8_t* frozen,
+                               int precision, double* energy, double* grad) {
+  return guard([&] {
+    need(eam && list, "null handle");
+    need(list->built, "EAM call before List::rebuild()");
+    list_set_atoms(list, eam->n_types, nullptr, nullptr, true, types, frozen);
+    std::size_t const n3 = 3 * static_cast<std::size_t>(list->n);
+    list->io.reserve(n3 + 3);
+    list->energy.reserve(1);
+    run_eam(eam, list, precision, energy ? list->energy.p : nullptr, grad ? list->io.p : nullptr);
+    if (grad && n3)
+      FLY_CUDA(cudaMemcpyAsync(grad, list->io.p, sizeof(double) * n3, cudaMemcpyDeviceToHost, list->stream));
+    if (energy) FLY_CUDA(cudaMemcpyAsync(energy, list->energy.p, sizeof(double), cudaMemcpyDeviceToHost, list->stream));
+    check_device(list);
+  });
+}
+
+int flygpu_eam_energy(flygpu_eam* eam, flygpu_list* list, const uint32_t* types, const uint8_t* frozen, int precision,
+                      double* energy) {
+  if (!energy) {
+    set_error("null energy pointer");
+    return FLYGPU_INVALID_ARG;
+  }
+  return flygpu_eam_energy_gradient(eam, list, types, frozen, precision, energy, nullptr);
+}
+
+int flygpu_eam_gradient(flygpu_eam* eam, flygpu_list* list, const uint32_t* types, const uint8_t* frozen,
+                        int precision, double* grad) {
+  if (!grad) {
+    set_error("null gradient pointer");
+    return FLYGPU_INVALID_ARG;
+  }
+  return flygpu_eam_energy_gradient(eam, list, types, frozen, precision, nullptr, grad);
+}
+
+int flygpu_eam_energy_gradient_device(flygpu_eam* eam, flygpu_list* list, const uint32_t* d_types,
+                                      const uint8_t* d_frozen, int precision, double* d_energy, double* d_grad) {
+  return guard([&] {
+    need(eam && list, "null handle");
+    need(list->built, "EAM call before List::rebuild()");
+    if (d_types || d_frozen || !list->types_set) list_set_atoms(list, eam->n_types, d_types, d_frozen, false, nullptr, nullptr);
+    run_eam(eam, list, precision, d_energy, d_grad);
+  });
+}
+
+}  // extern "C"

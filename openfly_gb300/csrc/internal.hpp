@@ -1,0 +1,233 @@
+// internal.hpp -- structures shared by the host and device translation units of libflygpu.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/flygpu.h"
+
+namespace flygpu {
+
+  // 32-byte aligned binary64 quadruple: a position (+ one scalar) or a spline interval {a, b, c, d};
+  // one 32-byte sector per access.
+  struct alignas(32) D4 {
+    double x, y, z, w;
+  };
+
+  // ------------------------------------------------------------------ errors
+
+  void set_error(std::string msg);
+
+  struct Error {
+    int status;
+    std::string msg;
+  };
+
+  [[noreturn]] void fail(int status, std::string msg);
+
+  inline void cuda_check(cudaError_t e, char const* what) {
+    if (e == cudaErrorMemoryAllocation) fail(FLYGPU_OOM, std::string(what) + ": " + cudaGetErrorString(e));
+    if (e != cudaSuccess) fail(FLYGPU_CUDA_ERROR, std::string(what) + ": " + cudaGetErrorString(e));
+  }
+
+#define FLY_CUDA(call) ::flygpu::cuda_check((call), #call)
+
+  // Device-side error word bits (one word per list handle). Kernels never trap: they set a bit and
+  // skip the offending access; the host turns the word into a status after the next sync.
+  enum : int {
+    ERR_SPLINE_OOB = 1,
+    ERR_NLIST_OVERFLOW = 2,
+    ERR_GHOST_OVERFLOW = 4,
+    ERR_BAD_INDEX = 8,
+    ERR_TIMEOUT = 16,
+  };
+
+  int status_from_word(int word);
+
+  // ------------------------------------------------------------------ device buffers
+
+  template <typename T>
+  struct DevBuf {
+    T* p = nullptr;
+    std::size_t n = 0;
+
+    DevBuf() = default;
+    DevBuf(DevBuf const&) = delete;
+    DevBuf& operator=(DevBuf const&) = delete;
+    ~DevBuf() { release(); }
+
+    void release() {
+      if (p) cudaFree(p);
+      p = nullptr;
+      n = 0;
+    }
+    // Grow to at least count elements; contents are not preserved.
+    void reserve(std::size_t count) {
+      if (count <= n) return;
+      release();
+      std::size_t want = count + count / 8 + 16;
+      FLY_CUDA(cudaMalloc(&p, want * sizeof(T)));
+      n = want;
+    }
+    // Grow to at least count elements keeping the first keep elements.
+    void grow_keep(std::size_t count, std::size_t keep, cudaStream_t s) {
+      if (count <= n) return;
+      T* q = nullptr;
+      std::size_t want = count + count / 4 + 16;
+      FLY_CUDA(cudaMalloc(&q, want * sizeof(T)));
+      if (p && keep) FLY_CUDA(cudaMemcpyAsync(q, p, keep * sizeof(T), cudaMemcpyDeviceToDevice, s));
+      FLY_CUDA(cudaStreamSynchronize(s));
+      if (p) cudaFree(p);
+      p = q;
+      n = want;
+    }
+  };
+
+  template <typename T>
+  struct PinnedBuf {
+    T* p = nullptr;
+    std::size_t n = 0;
+    PinnedBuf() = default;
+    PinnedBuf(PinnedBuf const&) = delete;
+    PinnedBuf& operator=(PinnedBuf const&) = delete;
+    ~PinnedBuf() {
+      if (p) cudaFreeHost(p);
+    }
+    void reserve(std::size_t count) {
+      if (count <= n) return;
+      if (p) cudaFreeHost(p);
+      p = nullptr;
+      FLY_CUDA(cudaMallocHost(&p, count * sizeof(T)));
+      n = count;
+    }
+  };
+
+  // ------------------------------------------------------------------ EAM tables
+
+  // Per function kind the device holds binary64 {a,b,c,d} per interval (reference form) and binary32
+  // coefficients of the same cubic in the interval's unit coordinate t = x/dx - i:
+  // f = a + t(b' + t(c' + t d')) with b' = b dx, c' = c dx^2, d' = d dx^3.
+  struct SplineSet {
+    int count = 0;        // number of functions of this kind
+    int n_spines = 0;     // intervals per function
+    double dx = 0, inv_dx = 0;
+    std::vector<double> host;  // count * n_spines * 4
+    DevBuf<D4> d64;
+    DevBuf<float4> d32;
+  };
+
+  // Device view passed to kernels by value.
+  struct TablesView {
+    int n_types;
+    int nP, nR;  // intervals of F and of phi / v
+    double dP, inv_dP, dR, inv_dR;
+    float fdP, finv_dP, fdR, finv_dR;
+    D4 const* F64;
+    D4 const* phi64;  // [a + n*b] * nR
+    D4 const* v64;    // both orders filled
+    float4 const* F32;
+    float4 const* phi32;
+    float4 const* v32;
+  };
+
+}  // namespace flygpu
+
+struct flygpu_eam {
+  int n_types = 0;
+  double r_cut = 0;
+  std::vector<std::string> names;
+  std::vector<double> mass;
+  flygpu::SplineSet F, phi, v;  // phi and v hold n*n functions (v symmetric, both orders)
+  flygpu::TablesView view() const;
+};
+
+namespace flygpu {
+
+  struct GridDesc {
+    double L[3];
+    double cell[3], inv_cell[3];
+    int shape[3];
+    int per[3];
+    double rc;  // list cut-off
+    int ncells() const { return shape[0] * shape[1] * shape[2]; }
+  };
+
+  // Binary32 slot record for the MIXED passes: the position as (hi, lo) pairs of an offset coordinate
+  // x + shift whose hi parts all lie in one binade, so hi differences are exact; plus the slot's type
+  // and its atom's F'(rho). 32 bytes, one sector per neighbour gather.
+  struct alignas(32) Packed {
+    float hx, hy, hz;
+    std::uint32_t type;
+    float lx, ly, lz;
+    float fp;
+  };
+
+}  // namespace flygpu
+
+struct flygpu_list {
+  flygpu::GridDesc g{};
+  double shift[3] = {0, 0, 0};  // offset of the binary32 packed coordinates
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+
+  std::int64_t n = 0;        // real atoms
+  std::int64_t n_slots = 0;  // real + ghost
+  int nb_cap = 0;            // neighbour capacity per atom
+  bool built = false;
+
+  // reference-order slots (real atoms then ghosts in List::make_ghosts order)
+  flygpu::DevBuf<flygpu::D4> r_ref;
+  flygpu::DevBuf<int> img_ref, cell_ref, flag_p, flag_m, scan_p, scan_m;
+  // physical (cell-sorted) slots
+  flygpu::DevBuf<flygpu::D4> pos;   // xyz + w = F'(rho) of the slot's atom (FP64 passes)
+  flygpu::DevBuf<int> pimg;      // real index of each physical slot
+  flygpu::DevBuf<int> pref;      // reference slot id of each physical slot
+  flygpu::DevBuf<int> ptype;     // type of each physical slot
+  flygpu::DevBuf<flygpu::Packed> packed;
+  flygpu::DevBuf<int> cell_count, cell_start, cell_fill, members;
+  flygpu::DevBuf<int> real_phys;  // physical slot of the j-th real atom in cell order
+  flygpu::DevBuf<int> nbr;        // [nb_cap][n] physical neighbour slots, column per atom
+  flygpu::DevBuf<int> ncount;
+  // per real atom
+  flygpu::DevBuf<std::uint32_t> types;
+  flygpu::DevBuf<std::uint8_t> frozen;
+  flygpu::DevBuf<double> fprime;   // F'(rho) by real index
+  flygpu::DevBuf<double> io;       // 3n staging for host copies
+  flygpu::DevBuf<double> energy_part;
+  flygpu::DevBuf<double> energy;   // 1
+  flygpu::DevBuf<int> scan_tmp;
+  flygpu::DevBuf<int> err;         // device error word
+  flygpu::DevBuf<int> counters;    // small device counters
+  flygpu::PinnedBuf<int> h_small;  // pinned mirror of counters / error word
+  flygpu::PinnedBuf<double> h_io;
+  bool types_set = false;
+  bool frozen_set = false;
+  bool packed_valid = false;
+};
+
+namespace flygpu {
+
+  // nlist.cu
+  void list_rebuild(flygpu_list* L, double const* d_pos, std::int64_t n);
+  void list_update(flygpu_list* L, double const* d_delta);
+  // n_types bounds the type indices (out-of-range types raise FLYGPU_INVALID_ARG).
+  void list_set_atoms(flygpu_list* L, int n_types, std::uint32_t const* d_types, std::uint8_t const* d_frozen,
+                      bool copy_from_host, std::uint32_t const* h_types, std::uint8_t const* h_frozen);
+  void list_pack(flygpu_list* L);
+  int list_take_error(flygpu_list* L);  // syncs, reads and clears the device error word
+  std::int64_t list_export(flygpu_list* L, double r_cut, int* counts, int* idx, double* dr, std::int64_t cap);
+  void exclusive_scan(int const* in, int* out, std::int64_t n, int* tmp, std::size_t tmp_len, cudaStream_t s);
+  std::size_t scan_tmp_size(std::int64_t n);
+
+  // eam_fp64.cu / eam_mixed.cu
+  void eam_fp64(flygpu_eam const* E, flygpu_list* L, double* d_energy, double* d_grad);
+  void eam_mixed(flygpu_eam const* E, flygpu_list* L, double* d_energy, double* d_grad);
+
+  // tables.cpp
+  void build_spline(std::vector<double> y, double dx, double* out4, int n_spines);
+  int spline_spines(std::size_t n_samples);
+
+}  // namespace flygpu

@@ -33,6 +33,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <exception>
 #include <fstream>
 #include <limits>
 #include <memory>
@@ -387,30 +388,56 @@ namespace orc {
 
     double r_cut() const { return d->rcut; }
 
+    // Runs body(i) for i in [0, n): a plain loop for one thread (so Spline::OutOfBounds propagates,
+    // as eam.cpp:75-86 arranges), else an OpenMP static loop that re-throws the first exception.
+    template <typename F>
+    static void loop(long n, int threads, F&& body) {
+      if (threads == 1) {
+        for (long i = 0; i < n; ++i) body(i);
+        return;
+      }
+      std::exception_ptr first;
+#pragma omp parallel for num_threads(threads) schedule(static)
+      for (long i = 0; i < n; ++i) {
+        try {
+          body(i);
+        } catch (...) {
+#pragma omp critical
+          if (!first) first = std::current_exception();
+        }
+      }
+      if (first) std::rethrow_exception(first);
+    }
+
     double energy(std::uint32_t const* t, List const& nl, int threads) const {
-      double v_sum = 0, f_sum = 0;
-#pragma omp parallel for reduction(+ : v_sum, f_sum) num_threads(threads) schedule(static)
-      for (long a = 0; a < nl.n; a++) {
-        double rho = 0;
+      // eam.cpp:33-51 reduces v and F over threads; partial sums per atom are combined in index order
+      // here so the result does not depend on the thread count.
+      std::vector<double> vs(static_cast<std::size_t>(nl.n)), fs(static_cast<std::size_t>(nl.n));
+      loop(nl.n, threads, [&](long a) {
+        double rho = 0, v = 0;
         nl.for_neighbours(a, r_cut(), [&](long b, double r, double const*) {
-          v_sum += d->v_of(t[a], t[b]).f(r);
+          v += d->v_of(t[a], t[b]).f(r);
           rho += d->phi_of(t[b], t[a]).f(r);
         });
-        f_sum += d->f_of(t[a]).f(rho);
+        vs[static_cast<std::size_t>(a)] = v;
+        fs[static_cast<std::size_t>(a)] = d->f_of(t[a]).f(rho);
+      });
+      double v_sum = 0, f_sum = 0;
+      for (long a = 0; a < nl.n; ++a) {
+        v_sum += vs[static_cast<std::size_t>(a)];
+        f_sum += fs[static_cast<std::size_t>(a)];
       }
       return (0.5 * v_sum) + f_sum;
     }
 
     void gradient(double* out, std::uint32_t const* t, std::uint8_t const* frozen, List const& nl, int threads) {
       fprime.resize(static_cast<std::size_t>(nl.n));
-#pragma omp parallel for num_threads(threads) schedule(static)
-      for (long b = 0; b < nl.n; b++) {
+      loop(nl.n, threads, [&](long b) {
         double rho = 0;
         nl.for_neighbours(b, r_cut(), [&](long a, double r, double const*) { rho += d->phi_of(t[a], t[b]).f(r); });
         fprime[static_cast<std::size_t>(b)] = d->f_of(t[b]).fp(rho);
-      }
-#pragma omp parallel for num_threads(threads) schedule(static)
-      for (long g = 0; g < nl.n; ++g) {
+      });
+      loop(nl.n, threads, [&](long g) {
         double grad[3] = {0, 0, 0};
         if (!frozen[g]) {
           nl.for_neighbours(g, r_cut(), [&](long a, double r, double const* dr) {
@@ -421,7 +448,7 @@ namespace orc {
           });
         }
         for (int k = 0; k < 3; ++k) out[3 * g + k] = grad[k];
-      }
+      });
     }
   };
 
