@@ -1,0 +1,353 @@
+#!/usr/bin/env python
+"""Throughput of the openFLY saddle-search inner loop on GB300.
+
+Workload (one "step"): on 80^3 bcc Fe (1,024,000 sites, 0.1 % vacancies, 0.05 % H on tetrahedral
+sites, sigma = 0.05 A noise; 1,023,487 atoms), a neighbour-list update with a 0.3 A skin followed by
+one EAM energy + gradient evaluation (binary32 pair terms, binary64 accumulation). Each step applies a
+resident displacement field of at most 0.005 A per atom (alternating +D_j, -D_j); the list is rebuilt
+whenever the accumulated maximum displacement exceeds skin / 2 (the reference's rule,
+src/minimise/LBFGS/lbfgs.cpp:96-101), and those rebuilds are inside the timed region.
+
+value: atom-evals/s with inputs resident in HBM (device-timed with CUDA events on the library's
+stream). e2e: the same steps through the host C ABI (flygpu_list_update / flygpu_eam_energy_gradient
+with pinned host buffers: H2D of the displacement, D2H of gradient and energy every step).
+
+--impl reference times the reference's CPU path for the same workload: the oracle port (the reference
+cannot be compiled here: Eigen, fmt and its other dependencies are absent) with every host thread.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+SKIN = 0.3
+STEP_DISP = 0.005  # max per-atom displacement per step (A)
+N_FIELDS = 4
+ALGO_BYTES_DENSITY = 36  # per atom: 24 B position + 4 B type read, 8 B F' write
+ALGO_BYTES_FORCE = 60    # per atom: 24 B position + 4 B type + 8 B F' read, 24 B gradient write
+ALGO_BYTES_STEP = 168    # per atom and step: 96 B EAM (both passes) + 72 B list update
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def make_workload(cells: int):
+    from openfly_gb300 import workloads as W
+
+    s = W.config2(n_cells=cells)
+    rng = np.random.default_rng(99)
+    fields = []
+    for _ in range(N_FIELDS):
+        d = rng.normal(0.0, 1.0, s.pos.shape)
+        d *= STEP_DISP / np.linalg.norm(d, axis=1).max()
+        fields.append(d)
+    return s, fields
+
+
+def schedule(steps: int):
+    """(field index, sign, rebuild-after-update?) per step, with the reference's skin rule."""
+    acc, out = 0.0, []
+    for k in range(steps):
+        j, sign = (k // 2) % N_FIELDS, (1.0 if k % 2 == 0 else -1.0)
+        acc += STEP_DISP
+        rebuild = acc > 0.5 * SKIN
+        if rebuild:
+            acc = 0.0
+        out.append((j, sign, rebuild))
+    return out
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int = 0):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={index}", f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                      stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self) -> dict | None:
+        if self.p is None:
+            return None
+        self.p.terminate()
+        self.p.wait()
+        self.f.flush()
+        rows = [r.split(",") for r in open(self.f.name).read().strip().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                mx = max(mx, float(r[2]))
+                for name, v in zip(names, r[5:9]):
+                    if v.strip() == "Active":
+                        reasons.add(name)
+            except (ValueError, IndexError):
+                continue
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak_hbm() -> tuple[float, str]:
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        return float(json.load(open(p))["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def traffic_from_profile(kernel: str) -> float | None:
+    p = os.path.join(ROOT, "profiles", "c2_dram_traffic.json")
+    if os.path.exists(p):
+        return json.load(open(p)).get(kernel)
+    return None
+
+
+# ----------------------------------------------------------------------------- CPU (oracle) leg
+
+def cpu_c2(s, fields, steps: int, threads: int):
+    """The reference's CPU path (oracle port) on the same steps; returns (seconds, steps, rebuilds)."""
+    from oracle import pyoracle as O
+    from openfly_gb300 import workloads as W
+
+    data = O.EAMData(W.TABLE)
+    nl = O.List(s.extents, s.periodic, data.r_cut + SKIN)
+    nl.rebuild(s.pos, threads)
+    sched = schedule(steps)
+    pos_alt = [s.pos - f for f in fields]
+    t0 = time.perf_counter()
+    rebuilds = 0
+    for j, sign, rb in sched:
+        if rb:
+            nl.rebuild(pos_alt[j] if sign > 0 else s.pos, threads)
+            rebuilds += 1
+        else:
+            nl.update(sign * fields[j])
+        O.eam_energy(data, nl, s.types, threads)
+        O.eam_gradient(data, nl, s.types, s.frozen, threads)
+    return time.perf_counter() - t0, len(sched), rebuilds
+
+
+def reference_arm(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    s, fields = make_workload(args.cells)
+    from oracle import pyoracle as O
+
+    O.build()
+    os.environ.setdefault("OMP_NUM_THREADS", str(threads))
+    # warm-up then K timed steps, each a full step of the workload on every host thread
+    cpu_c2(s, fields, max(1, args.warmup), threads)
+    secs, k, rb = cpu_c2(s, fields, args.steps, threads)
+    value = s.n * k / secs
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "atom-evals/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / k, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": config_dict(s, args),
+        "cpu_baseline": {"value": value, "unit": "atom-evals/s", "cores": threads, "kind": "port",
+                         "sample": f"{k} full steps ({rb} rebuilds) of the {s.n}-atom workload"},
+        "e2e": {"value": value, "unit": "atom-evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+METRIC = "saddle searches/s + p50/p99 latency vs one-at-a-time GPU @<=1 meV; atom-evals/s"
+
+
+def config_dict(s, args):
+    return {"workload": f"config 2: {args.cells}^3 bcc Fe, 0.1% vacancies, 0.05% H, sigma 0.05 A; per step "
+                        f"List::update (skin {SKIN} A, rebuild by the reference's skin rule) + EAM energy+gradient",
+            "atoms": s.n, "cells": args.cells, "precision": "binary32 pairs / binary64 accumulation",
+            "l2": "inputs larger than L2 (positions, packed slots, neighbour columns ~0.4 GB)",
+            "parallelism": f"replicas x{args.gpus}"}
+
+
+# ----------------------------------------------------------------------------- GPU leg
+
+def ours(args):
+    import torch
+
+    import openfly_gb300 as fly
+    from openfly_gb300 import workloads as W
+    from openfly_gb300.build import build
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = world > 1
+    if dist:
+        import torch.distributed as tdist
+
+        tdist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    if rank == 0 or not dist:
+        build()
+    if dist:
+        tdist.barrier()
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.current_stream(dev)
+
+    s, fields = make_workload(args.cells)
+    n = s.n
+    eam = fly.EAM(W.TABLE)
+    nl = fly.List(s.extents, s.periodic, eam.r_cut() + SKIN, stream=stream.cuda_stream)
+    d_fields = [torch.from_numpy(f.reshape(-1)).to(dev) for f in fields]
+    d_neg = [-f for f in d_fields]
+    d_pos0 = torch.from_numpy(s.pos.reshape(-1)).to(dev)
+    d_pos_alt = [d_pos0 - f for f in d_fields]
+    d_types = torch.from_numpy(s.types.astype(np.int32)).to(dev)
+    d_frozen = torch.from_numpy(s.frozen).to(dev)
+    d_grad = torch.empty(3 * n, dtype=torch.float64, device=dev)
+    d_e = torch.empty(1, dtype=torch.float64, device=dev)
+    nl.rebuild_device(d_pos0, n)
+    eam.energy_gradient_device(nl, d_e, d_grad, d_types=d_types, d_frozen=d_frozen, precision=fly.MIXED)
+    nl.sync()
+
+    def step(j, sign, rb):
+        if rb:
+            nl.rebuild_device(d_pos_alt[j] if sign > 0 else d_pos0, n)
+        else:
+            nl.update_device(d_fields[j] if sign > 0 else d_neg[j])
+        eam.energy_gradient_device(nl, d_e, d_grad, precision=fly.MIXED)
+
+    for j, sign, rb in schedule(args.warmup):
+        step(j, sign, rb)
+    nl.sync()
+    sched = schedule(args.steps)
+    if dist:
+        tdist.barrier()
+    torch.cuda.synchronize()
+    clocks = Clocks(local)
+    nl.set_timing(True)
+    launches0 = fly.launch_count()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for j, sign, rb in sched:
+        step(j, sign, rb)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    launches = fly.launch_count() - launches0
+    ktimes = nl.kernel_times()
+    clk = clocks.stop()
+    nl.sync()
+    ms = ev0.elapsed_time(ev1)
+    if dist:
+        t = torch.tensor([ms], device=dev)
+        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = n * world * args.steps / (ms * 1e-3)
+
+    # e2e through the host C ABI with pinned host buffers
+    h_fields = [torch.from_numpy(f.reshape(-1)).pin_memory() for f in fields]
+    h_neg = [(-f).pin_memory() for f in h_fields]
+    h_pos0 = torch.from_numpy(s.pos.reshape(-1)).pin_memory()
+    h_pos_alt = [(h_pos0 - f).pin_memory() for f in h_fields]
+    h_grad = torch.empty(3 * n, dtype=torch.float64).pin_memory()
+    h_types, h_frozen = s.types, s.frozen
+    nl.rebuild(h_pos0.numpy())
+    eam.energy_gradient(h_types, h_frozen, nl, fly.MIXED, out=h_grad.numpy())
+
+    def step_host(j, sign, rb):
+        if rb:
+            nl.rebuild((h_pos_alt[j] if sign > 0 else h_pos0).numpy())
+        else:
+            nl.update((h_fields[j] if sign > 0 else h_neg[j]).numpy())
+        return eam.energy_gradient(None, None, nl, fly.MIXED, out=h_grad.numpy())[0]
+
+    for j, sign, rb in schedule(args.warmup):
+        step_host(j, sign, rb)
+    if dist:
+        tdist.barrier()
+    t0 = time.perf_counter()
+    for j, sign, rb in sched:
+        step_host(j, sign, rb)
+    e2e_s = time.perf_counter() - t0
+    if dist:
+        t = torch.tensor([e2e_s], device=dev)
+        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    n_rb = sum(1 for _, _, rb in sched if rb)
+    h2d = 24 * n  # a displacement field, or the positions on rebuild steps
+    d2h = 24 * n + 8
+
+    # roofline of the dominant kernel
+    peak, peak_kind = measured_peak_hbm()
+    f_ms, f_cnt = ktimes["force"]
+    d_ms, d_cnt = ktimes["density"]
+    dom = "force" if f_ms >= d_ms else "density"
+    dom_ms, dom_cnt = ktimes[dom]
+    per_atom = ALGO_BYTES_FORCE if dom == "force" else ALGO_BYTES_DENSITY
+    achieved = per_atom * n / (dom_ms / dom_cnt * 1e-3) / 1e9
+    traffic = traffic_from_profile("k_force32" if dom == "force" else "k_density32")
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "atom-evals/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 pair terms / f64 accumulation", "data": "synthetic",
+        "config": config_dict(s, args),
+        "e2e": {"value": n * world * args.steps / e2e_s, "unit": "atom-evals/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h)},
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
+                     "algorithmic_bytes_per_atom": per_atom},
+        "kernel_ms_per_step": {k: v[0] / max(1, args.steps) for k, v in ktimes.items()},
+        "step_algorithmic_GBps": ALGO_BYTES_STEP * n * args.steps / (ms * 1e-3) / 1e9,
+        "gpu_launches": int(launches),
+        "clocks": clk,
+    }
+    if rank == 0 and not args.no_cpu and world == 1:
+        threads = os.cpu_count() or 1
+        os.environ.setdefault("OMP_NUM_THREADS", str(threads))
+        secs, k, rb = cpu_c2(s, fields, args.cpu_steps, threads)
+        line["cpu_baseline"] = {"value": n * k / secs, "unit": "atom-evals/s", "cores": threads, "kind": "port",
+                                "sample": f"{k} steps ({rb} rebuild) of the same {n}-atom workload, oracle port, "
+                                          f"{threads} OpenMP threads"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist:
+        tdist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=60)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--cells", type=int, default=80, help="bcc cells per side (80 -> 1,024,000 sites)")
+    ap.add_argument("--cpu-steps", type=int, default=3, help="steps of the bounded CPU baseline sample")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be at least 3")
+    if args.impl == "reference":
+        reference_arm(args)
+    else:
+        ours(args)
+
+
+if __name__ == "__main__":
+    main()

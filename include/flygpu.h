@@ -51,6 +51,9 @@ typedef struct flygpu_server flygpu_server;
 const char* flygpu_status_string(int status);
 /* Message of the last failing call on this host thread ("" if none). */
 const char* flygpu_last_error(void);
+/* Number of CUDA kernels this library has launched since it was loaded (all threads). No reference
+ * counterpart: instrumentation for throughput accounting. */
+int64_t flygpu_launch_count(void);
 
 /* ---------------------------------------------------------------- EAM tables
  * Replaces DataEAM::DataEAM (potential/EAM/data.hpp:54, src/potential/EAM/data.cpp:67-153): parses a
@@ -86,6 +89,12 @@ int64_t flygpu_list_num_ghosts(const flygpu_list* list);
  * minus atom). total receives the pair count; idx/dr are filled when cap >= total. */
 int flygpu_list_neighbours(flygpu_list* list, double r_cut, int32_t* counts, int32_t* idx, double* dr,
                            int64_t cap, int64_t* total);
+/* Per-kernel CUDA-event timing on the list's stream (no reference counterpart; the reference's only
+ * instrumentation is timeit(), utility/core.hpp:888-921). Enabling clears earlier records.
+ * kernel_times fills ms[4] / counts[4] for {density pass, force pass, update, rebuild} since the last
+ * call and clears them. */
+int flygpu_list_set_timing(flygpu_list* list, int enable);
+int flygpu_list_kernel_times(flygpu_list* list, double* ms, int64_t* counts);
 /* Wait for the list's stream and report the first device-side error raised since the last call. */
 int flygpu_list_sync(flygpu_list* list);
 

@@ -69,6 +69,9 @@ def lib() -> C.CDLL:
     L.flygpu_list_num_ghosts.argtypes = [V]
     L.flygpu_list_neighbours.argtypes = [V, C.c_double, V, V, V, I64, C.POINTER(I64)]
     L.flygpu_list_sync.argtypes = [V]
+    L.flygpu_list_set_timing.argtypes = [V, C.c_int]
+    L.flygpu_list_kernel_times.argtypes = [V, V, V]
+    L.flygpu_launch_count.restype = I64
     for name in ("flygpu_eam_energy",):
         getattr(L, name).argtypes = [V, V, V, V, C.c_int, V]
     L.flygpu_eam_gradient.argtypes = [V, V, V, V, C.c_int, V]
@@ -76,6 +79,11 @@ def lib() -> C.CDLL:
     L.flygpu_eam_energy_gradient_device.argtypes = [V, V, V, V, C.c_int, V, V]
     _lib = L
     return L
+
+
+def launch_count() -> int:
+    """Kernels libflygpu has launched since it was loaded."""
+    return lib().flygpu_launch_count()
 
 
 def status_string(status: int) -> str:
@@ -207,6 +215,19 @@ class List:
 
     def sync(self) -> None:
         check(lib().flygpu_list_sync(self.h), "List sync")
+
+    KERNELS = ("density", "force", "update", "rebuild")
+
+    def set_timing(self, enable: bool) -> None:
+        """Record CUDA events around the density, force, update and rebuild kernels."""
+        check(lib().flygpu_list_set_timing(self.h, int(enable)), "set_timing")
+
+    def kernel_times(self) -> dict:
+        """{kernel: (total ms, launches)} since the last call; synchronises the list's stream."""
+        ms = np.zeros(4, dtype=np.float64)
+        cnt = np.zeros(4, dtype=np.int64)
+        check(lib().flygpu_list_kernel_times(self.h, ms.ctypes.data, cnt.ctypes.data), "kernel_times")
+        return {k: (float(ms[i]), int(cnt[i])) for i, k in enumerate(self.KERNELS)}
 
     def neighbours(self, r_cut: float):
         """(counts, real indices, dr) of every pair List::for_neighbours visits, in visiting order."""

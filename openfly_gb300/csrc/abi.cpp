@@ -1,5 +1,6 @@
 // abi.cpp -- extern "C" entry points of libflygpu (declared in include/flygpu.h).
 
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <memory>
@@ -11,7 +12,11 @@ namespace flygpu {
 
   namespace {
     thread_local std::string g_last_error;
+    std::atomic<long long> g_launches{0};
   }
+
+  void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+  long long launch_count() { return g_launches.load(std::memory_order_relaxed); }
 
   void set_error(std::string msg) { g_last_error = std::move(msg); }
 
@@ -27,6 +32,22 @@ namespace flygpu {
   }
 
   flygpu_eam* eam_load(char const* path);
+
+  cudaEvent_t timer_record(flygpu_list* L) {
+    if (!L->timing) return nullptr;
+    if (L->ev_used == L->ev_pool.size()) {
+      cudaEvent_t e;
+      FLY_CUDA(cudaEventCreate(&e));
+      L->ev_pool.push_back(e);
+    }
+    cudaEvent_t const e = L->ev_pool[L->ev_used++];
+    FLY_CUDA(cudaEventRecord(e, L->stream));
+    return e;
+  }
+
+  void timer_mark(flygpu_list* L, int kind, cudaEvent_t a, cudaEvent_t b) {
+    if (a && b) L->marks.push_back({kind, a, b});
+  }
 
   // Runs f, converting exceptions into a status and recording the message.
   template <typename F>
@@ -91,6 +112,8 @@ const char* flygpu_status_string(int status) {
 }
 
 const char* flygpu_last_error(void) { return g_last_error.c_str(); }
+
+int64_t flygpu_launch_count(void) { return launch_count(); }
 
 int flygpu_eam_load(const char* path, flygpu_eam** out) {
   return guard([&] {
@@ -207,6 +230,35 @@ int flygpu_list_neighbours(flygpu_list* list, double r_cut, int32_t* counts, int
     need(list && total, "null argument");
     *total = list_export(list, r_cut, counts, idx, dr, cap);
     check_device(list);
+  });
+}
+
+int flygpu_list_set_timing(flygpu_list* list, int enable) {
+  return guard([&] {
+    need(list, "null handle");
+    FLY_CUDA(cudaStreamSynchronize(list->stream));
+    list->timing = enable != 0;
+    list->marks.clear();
+    list->ev_used = 0;
+  });
+}
+
+int flygpu_list_kernel_times(flygpu_list* list, double* ms, int64_t* counts) {
+  return guard([&] {
+    need(list && ms && counts, "null argument");
+    FLY_CUDA(cudaStreamSynchronize(list->stream));
+    for (int k = 0; k < TK_COUNT; ++k) {
+      ms[k] = 0;
+      counts[k] = 0;
+    }
+    for (auto const& m : list->marks) {
+      float t = 0;
+      FLY_CUDA(cudaEventElapsedTime(&t, m.a, m.b));
+      ms[m.kind] += t;
+      counts[m.kind] += 1;
+    }
+    list->marks.clear();
+    list->ev_used = 0;
   });
 }
 

@@ -200,22 +200,24 @@ namespace flygpu {
     double const rc2 = rc * rc;
     unsigned const nb = static_cast<unsigned>((n + T - 1) / T);
     L->fprime.reserve(static_cast<std::size_t>(n));
+    cudaEvent_t const t0 = timer_record(L);
     if (d_energy) {
       L->energy_part.reserve(2 * static_cast<std::size_t>(nb));
-      k_density<true><<<nb, T, 0, s>>>(tb, L->pos.p, L->ptype.p, L->pimg.p, L->real_phys.p, L->nbr.p, L->ncount.p, n, rc2,
+      launch(k_density<true>, nb, T, 0, s, tb, L->pos.p, L->ptype.p, L->pimg.p, L->real_phys.p, L->nbr.p, L->ncount.p, n, rc2,
                                        L->fprime.p, L->energy_part.p, L->err.p);
-      k_energy_final<<<1, 256, 0, s>>>(L->energy_part.p, static_cast<int>(nb), d_energy);
+      launch(k_energy_final, 1, 256, 0, s, L->energy_part.p, static_cast<int>(nb), d_energy);
     } else {
-      k_density<false><<<nb, T, 0, s>>>(tb, L->pos.p, L->ptype.p, L->pimg.p, L->real_phys.p, L->nbr.p, L->ncount.p, n,
+      launch(k_density<false>, nb, T, 0, s, tb, L->pos.p, L->ptype.p, L->pimg.p, L->real_phys.p, L->nbr.p, L->ncount.p, n,
                                         rc2, L->fprime.p, nullptr, L->err.p);
     }
-    FLY_CUDA(cudaGetLastError());
+    timer_mark(L, TK_DENSITY, t0, timer_record(L));
     if (!d_grad) return;
-    k_fprime_slots<<<static_cast<unsigned>((L->n_slots + 255) / 256), 256, 0, s>>>(L->pos.p, L->pimg.p, L->n_slots,
+    launch(k_fprime_slots, static_cast<unsigned>((L->n_slots + 255) / 256), 256, 0, s, L->pos.p, L->pimg.p, L->n_slots,
                                                                                    L->fprime.p);
-    k_force<<<nb, T, 0, s>>>(tb, L->pos.p, L->ptype.p, L->pimg.p, L->real_phys.p, L->nbr.p, L->ncount.p, n, rc2,
+    cudaEvent_t const t1 = timer_record(L);
+    launch(k_force, nb, T, 0, s, tb, L->pos.p, L->ptype.p, L->pimg.p, L->real_phys.p, L->nbr.p, L->ncount.p, n, rc2,
                              L->frozen.p, d_grad, L->err.p);
-    FLY_CUDA(cudaGetLastError());
+    timer_mark(L, TK_FORCE, t1, timer_record(L));
   }
 
 }  // namespace flygpu

@@ -47,6 +47,21 @@ namespace flygpu {
 
   int status_from_word(int word);
 
+  // ------------------------------------------------------------------ launches
+
+  // Kernel launches made by this library since load (all go through launch()).
+  void count_launch();
+  long long launch_count();
+
+#ifdef __CUDACC__
+  template <typename... KArgs, typename... Args>
+  inline void launch(void (*k)(KArgs...), dim3 grid, dim3 block, std::size_t smem, cudaStream_t s, Args&&... args) {
+    k<<<grid, block, smem, s>>>(static_cast<KArgs>(args)...);
+    count_launch();
+    cuda_check(cudaGetLastError(), "kernel launch");
+  }
+#endif
+
   // ------------------------------------------------------------------ device buffers
 
   template <typename T>
@@ -206,6 +221,18 @@ struct flygpu_list {
   bool types_set = false;
   bool frozen_set = false;
   bool packed_valid = false;
+  // CUDA-event timing of the main kernels (enabled by flygpu_list_set_timing)
+  bool timing = false;
+  std::vector<cudaEvent_t> ev_pool;
+  std::size_t ev_used = 0;
+  struct Mark {
+    int kind;
+    cudaEvent_t a, b;
+  };
+  std::vector<Mark> marks;
+  ~flygpu_list() {
+    for (cudaEvent_t e : ev_pool) cudaEventDestroy(e);
+  }
 };
 
 namespace flygpu {
@@ -221,6 +248,12 @@ namespace flygpu {
   std::int64_t list_export(flygpu_list* L, double r_cut, int* counts, int* idx, double* dr, std::int64_t cap);
   void exclusive_scan(int const* in, int* out, std::int64_t n, int* tmp, std::size_t tmp_len, cudaStream_t s);
   std::size_t scan_tmp_size(std::int64_t n);
+
+  // Kernel timing kinds recorded by the list handle.
+  enum : int { TK_DENSITY = 0, TK_FORCE = 1, TK_UPDATE = 2, TK_REBUILD = 3, TK_COUNT = 4 };
+  // Records an event on the list's stream when timing is on (returns nullptr otherwise).
+  cudaEvent_t timer_record(flygpu_list* L);
+  void timer_mark(flygpu_list* L, int kind, cudaEvent_t a, cudaEvent_t b);
 
   // eam_fp64.cu / eam_mixed.cu
   void eam_fp64(flygpu_eam const* E, flygpu_list* L, double* d_energy, double* d_grad);

@@ -362,10 +362,10 @@ namespace flygpu {
     if (n <= 0) return;
     std::int64_t const nb = (n + SCAN_B - 1) / SCAN_B;
     if (static_cast<std::size_t>(nb) > tmp_len) fail(FLYGPU_CUDA_ERROR, "scan scratch too small");
-    k_scan_block<<<static_cast<unsigned>(nb), SCAN_T, 0, s>>>(in, out, n, tmp);
+    launch(k_scan_block, static_cast<unsigned>(nb), SCAN_T, 0, s, in, out, n, tmp);
     if (nb > 1) {
       exclusive_scan(tmp, tmp, nb, tmp + nb, tmp_len - static_cast<std::size_t>(nb), s);
-      k_scan_add<<<static_cast<unsigned>(nb), SCAN_T, 0, s>>>(out, n, tmp);
+      launch(k_scan_add, static_cast<unsigned>(nb), SCAN_T, 0, s, out, n, tmp);
     }
     FLY_CUDA(cudaGetLastError());
   }
@@ -391,11 +391,12 @@ namespace flygpu {
       L->built = true;
       return;
     }
+    cudaEvent_t const t_start = timer_record(L);
     std::int64_t const cap_slots = n * 27;  // real + MAX_GHOST_RATIO * n (neigh/list.hpp:78)
     std::size_t guess = static_cast<std::size_t>(n + n / 2 + 1024);
     L->r_ref.reserve(guess);
     L->img_ref.reserve(guess);
-    k_canon<<<blocks_for(n), T, 0, s>>>(d_pos, n, g, L->r_ref.p, L->img_ref.p, 1.0 / g.L[0], 1.0 / g.L[1], 1.0 / g.L[2]);
+    launch(k_canon, blocks_for(n), T, 0, s, d_pos, n, g, L->r_ref.p, L->img_ref.p, 1.0 / g.L[0], 1.0 / g.L[1], 1.0 / g.L[2]);
     FLY_CUDA(cudaGetLastError());
     std::int64_t slots = n;
     for (int ax = 0; ax < 3; ++ax) {
@@ -406,10 +407,10 @@ namespace flygpu {
       L->scan_p.reserve(static_cast<std::size_t>(end));
       L->scan_m.reserve(static_cast<std::size_t>(end));
       L->scan_tmp.reserve(scan_tmp_size(end));
-      k_ghost_flags<<<blocks_for(end), T, 0, s>>>(L->r_ref.p, end, ax, g.rc, g.L[ax], L->flag_p.p, L->flag_m.p);
+      launch(k_ghost_flags, blocks_for(end), T, 0, s, L->r_ref.p, end, ax, g.rc, g.L[ax], L->flag_p.p, L->flag_m.p);
       exclusive_scan(L->flag_p.p, L->scan_p.p, end, L->scan_tmp.p, L->scan_tmp.n, s);
       exclusive_scan(L->flag_m.p, L->scan_m.p, end, L->scan_tmp.p, L->scan_tmp.n, s);
-      k_totals<<<1, 1, 0, s>>>(L->flag_p.p, L->scan_p.p, L->flag_m.p, L->scan_m.p, end, L->counters.p);
+      launch(k_totals, 1, 1, 0, s, L->flag_p.p, L->scan_p.p, L->flag_m.p, L->scan_m.p, end, L->counters.p);
       FLY_CUDA(cudaGetLastError());
       sync_small(L, 2);
       std::int64_t const tp = L->h_small.p[0], tm = L->h_small.p[1];
@@ -418,7 +419,7 @@ namespace flygpu {
         fail(FLYGPU_GHOST_OVERFLOW, "more than MAX_GHOST_RATIO * n ghost atoms");
       L->r_ref.grow_keep(static_cast<std::size_t>(next), static_cast<std::size_t>(end), s);
       L->img_ref.grow_keep(static_cast<std::size_t>(next), static_cast<std::size_t>(end), s);
-      k_ghost_write<<<blocks_for(end), T, 0, s>>>(L->r_ref.p, L->img_ref.p, end, ax, g.L[ax], L->flag_p.p, L->scan_p.p,
+      launch(k_ghost_write, blocks_for(end), T, 0, s, L->r_ref.p, L->img_ref.p, end, ax, g.L[ax], L->flag_p.p, L->scan_p.p,
                                                   L->flag_m.p, L->scan_m.p, static_cast<int>(tp));
       FLY_CUDA(cudaGetLastError());
       slots = next;
@@ -433,10 +434,10 @@ namespace flygpu {
     L->scan_tmp.reserve(scan_tmp_size(std::max<std::int64_t>(nc, slots)));
     FLY_CUDA(cudaMemsetAsync(L->cell_count.p, 0, sizeof(int) * static_cast<std::size_t>(nc), s));
     FLY_CUDA(cudaMemsetAsync(L->cell_fill.p, 0, sizeof(int) * static_cast<std::size_t>(nc), s));
-    k_cell_index<<<blocks_for(slots), T, 0, s>>>(L->r_ref.p, slots, g, L->cell_ref.p, L->cell_count.p);
+    launch(k_cell_index, blocks_for(slots), T, 0, s, L->r_ref.p, slots, g, L->cell_ref.p, L->cell_count.p);
     exclusive_scan(L->cell_count.p, L->cell_start.p, nc, L->scan_tmp.p, L->scan_tmp.n, s);
-    k_cell_scatter<<<blocks_for(slots), T, 0, s>>>(L->cell_ref.p, slots, L->cell_start.p, L->cell_fill.p, L->members.p);
-    k_cell_sort<<<blocks_for(nc, 128), 128, 0, s>>>(L->cell_start.p, L->cell_count.p, nc, L->members.p);
+    launch(k_cell_scatter, blocks_for(slots), T, 0, s, L->cell_ref.p, slots, L->cell_start.p, L->cell_fill.p, L->members.p);
+    launch(k_cell_sort, blocks_for(nc, 128), 128, 0, s, L->cell_start.p, L->cell_count.p, nc, L->members.p);
     FLY_CUDA(cudaGetLastError());
     L->pos.reserve(static_cast<std::size_t>(slots));
     L->pimg.reserve(static_cast<std::size_t>(slots));
@@ -445,10 +446,10 @@ namespace flygpu {
     L->flag_p.reserve(static_cast<std::size_t>(slots));
     L->scan_p.reserve(static_cast<std::size_t>(slots));
     L->real_phys.reserve(static_cast<std::size_t>(n));
-    k_gather_phys<<<blocks_for(slots), T, 0, s>>>(L->members.p, slots, n, L->r_ref.p, L->img_ref.p, L->pos.p, L->pimg.p,
+    launch(k_gather_phys, blocks_for(slots), T, 0, s, L->members.p, slots, n, L->r_ref.p, L->img_ref.p, L->pos.p, L->pimg.p,
                                                    L->pref.p, L->flag_p.p);
     exclusive_scan(L->flag_p.p, L->scan_p.p, slots, L->scan_tmp.p, L->scan_tmp.n, s);
-    k_real_compact<<<blocks_for(slots), T, 0, s>>>(L->flag_p.p, L->scan_p.p, slots, L->real_phys.p);
+    launch(k_real_compact, blocks_for(slots), T, 0, s, L->flag_p.p, L->scan_p.p, slots, L->real_phys.p);
     FLY_CUDA(cudaGetLastError());
     // Neighbour lists; grow the capacity once if any atom overflowed it.
     L->ncount.reserve(static_cast<std::size_t>(n));
@@ -456,7 +457,7 @@ namespace flygpu {
     for (int attempt = 0; attempt < 2; ++attempt) {
       L->nbr.reserve(static_cast<std::size_t>(L->nb_cap) * static_cast<std::size_t>(n));
       FLY_CUDA(cudaMemsetAsync(L->counters.p + 2, 0, sizeof(int), s));
-      k_build<<<blocks_for(n, 128), 128, 0, s>>>(L->pos.p, L->real_phys.p, L->cell_ref.p, L->pref.p, L->cell_start.p,
+      launch(k_build, blocks_for(n, 128), 128, 0, s, L->pos.p, L->real_phys.p, L->cell_ref.p, L->pref.p, L->cell_start.p,
                                                  L->cell_count.p, n, g, L->nb_cap, L->nbr.p, L->ncount.p,
                                                  L->counters.p + 2);
       FLY_CUDA(cudaGetLastError());
@@ -467,9 +468,10 @@ namespace flygpu {
       L->nb_cap = (need + 7) / 8 * 8;
     }
     if (L->types_set) {
-      k_types_phys<<<blocks_for(slots), T, 0, s>>>(L->pimg.p, slots, L->types.p, 0, L->ptype.p, L->err.p);
+      launch(k_types_phys, blocks_for(slots), T, 0, s, L->pimg.p, slots, L->types.p, 0, L->ptype.p, L->err.p);
       FLY_CUDA(cudaGetLastError());
     }
+    timer_mark(L, TK_REBUILD, t_start, timer_record(L));
     L->built = true;
   }
 
@@ -477,8 +479,10 @@ namespace flygpu {
     if (!L->built) fail(FLYGPU_INVALID_ARG, "update() before rebuild()");
     if (L->n_slots == 0) return;
     Packed* pk = L->packed_valid ? L->packed.p : nullptr;
-    k_update<<<blocks_for(L->n_slots), T, 0, L->stream>>>(L->pos.p, L->pimg.p, L->n_slots, d_delta, pk, L->shift[0],
+    cudaEvent_t const t0 = timer_record(L);
+    launch(k_update, blocks_for(L->n_slots), T, 0, L->stream, L->pos.p, L->pimg.p, L->n_slots, d_delta, pk, L->shift[0],
                                                            L->shift[1], L->shift[2]);
+    timer_mark(L, TK_UPDATE, t0, timer_record(L));
     FLY_CUDA(cudaGetLastError());
   }
 
@@ -512,7 +516,7 @@ namespace flygpu {
       L->frozen_set = true;
     }
     if (types_changed && L->n_slots > 0) {
-      k_types_phys<<<blocks_for(L->n_slots), T, 0, L->stream>>>(L->pimg.p, L->n_slots, L->types.p, n_types,
+      launch(k_types_phys, blocks_for(L->n_slots), T, 0, L->stream, L->pimg.p, L->n_slots, L->types.p, n_types,
                                                                 L->ptype.p, L->err.p);
       FLY_CUDA(cudaGetLastError());
       L->packed_valid = false;
@@ -523,7 +527,7 @@ namespace flygpu {
   void list_pack(flygpu_list* L) {
     if (L->packed_valid || L->n_slots == 0) return;
     L->packed.reserve(static_cast<std::size_t>(L->n_slots));
-    k_pack<<<blocks_for(L->n_slots), T, 0, L->stream>>>(L->pos.p, L->ptype.p, L->n_slots, L->packed.p, L->shift[0],
+    launch(k_pack, blocks_for(L->n_slots), T, 0, L->stream, L->pos.p, L->ptype.p, L->n_slots, L->packed.p, L->shift[0],
                                                          L->shift[1], L->shift[2]);
     FLY_CUDA(cudaGetLastError());
     L->packed_valid = true;
@@ -550,7 +554,7 @@ namespace flygpu {
     DevBuf<long long> d_offs;
     DevBuf<double> d_dr;
     d_counts.reserve(static_cast<std::size_t>(n));
-    k_export_count<<<blocks_for(n), T, 0, s>>>(L->pos.p, L->real_phys.p, L->pimg.p, L->nbr.p, L->ncount.p, n, rc2,
+    launch(k_export_count, blocks_for(n), T, 0, s, L->pos.p, L->real_phys.p, L->pimg.p, L->nbr.p, L->ncount.p, n, rc2,
                                                d_counts.p);
     FLY_CUDA(cudaGetLastError());
     std::vector<int> hc(static_cast<std::size_t>(n));
@@ -568,7 +572,7 @@ namespace flygpu {
       d_idx.reserve(static_cast<std::size_t>(total));
       d_dr.reserve(static_cast<std::size_t>(3 * total));
       FLY_CUDA(cudaMemcpyAsync(d_offs.p, offs.data(), sizeof(long long) * offs.size(), cudaMemcpyHostToDevice, s));
-      k_export_fill<<<blocks_for(n), T, 0, s>>>(L->pos.p, L->real_phys.p, L->pimg.p, L->nbr.p, L->ncount.p, n, rc2,
+      launch(k_export_fill, blocks_for(n), T, 0, s, L->pos.p, L->real_phys.p, L->pimg.p, L->nbr.p, L->ncount.p, n, rc2,
                                                 d_offs.p, d_idx.p, d_dr.p);
       FLY_CUDA(cudaGetLastError());
       FLY_CUDA(cudaMemcpyAsync(idx, d_idx.p, sizeof(int) * static_cast<std::size_t>(total), cudaMemcpyDeviceToHost, s));
