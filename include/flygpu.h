@@ -114,6 +114,87 @@ int flygpu_eam_energy_gradient_device(flygpu_eam* eam, flygpu_list* list, const 
                                       const uint8_t* d_frozen, int precision, double* d_energy,
                                       double* d_grad);
 
+/* ---------------------------------------------------------------- searches */
+
+/* Dimer::Options (saddle/dimer.hpp:56-98) then Rotor::Options (saddle/rotor.hpp:47-60). */
+typedef struct {
+  int n, max_steps, hist_check_freq, use_history;
+  double f2norm, skin_frac, proj_tol, max_trust, min_trust, grow_trust, shrink_trust, convex_max;
+  int rot_n, iter_max_rot, relax_in_convex, pad_;
+  double delta_r, theta_tol;
+} flygpu_dimer_options;
+
+/* LBFGS::Options (minimise/LBFGS/lbfgs.hpp:56-80). */
+typedef struct {
+  int n, iter_max;
+  double f2norm, skin_frac, proj_tol, max_trust, min_trust, grow_trust, shrink_trust;
+} flygpu_lbfgs_options;
+
+/* The reference's defaults. */
+void flygpu_dimer_options_default(flygpu_dimer_options* opt);
+void flygpu_lbfgs_options_default(flygpu_lbfgs_options* opt);
+
+enum flygpu_search_mode { FLYGPU_SEARCH_DIMER = 0, FLYGPU_SEARCH_MINIMISE = 1 };
+
+/* One search: the arguments of Dimer::find_sp (saddle/dimer.hpp:148-155) or LBFGS::minimise
+ * (minimise/LBFGS/lbfgs.hpp:115-118) for one system. Host arrays; copied by the call taking them. */
+typedef struct {
+  int64_t n;               /* atoms */
+  const double* pos;       /* 3n Position */
+  const double* axis;      /* 3n Axis (dimer); NULL for a minimisation */
+  const uint32_t* types;   /* n TypeID */
+  const uint8_t* frozen;   /* n Frozen */
+  double extents[3];       /* orthorhombic box */
+  int periodic[3];
+  int mode;                /* flygpu_search_mode */
+  int n_hist;              /* previously found saddle points (hist_sp, dimer.cpp:102-131) */
+  const double* hist;      /* n_hist * 3n */
+  const double* in_min;    /* 3n minimum the dimer climbs from; NULL = pos */
+  double theta_tol;        /* collision angle in radians (find.cpp:692) */
+} flygpu_search_desc;
+
+typedef struct {
+  int exit_code;     /* Dimer::Exit, or for a minimisation 0 = converged, 1 = not (lbfgs.cpp:114) */
+  int status;        /* FLYGPU_* status of this search */
+  int steps;         /* translation / minimiser steps taken */
+  int pad_;
+  int64_t grad_calls; /* EAM gradient evaluations */
+  double curvature;  /* last dimer curvature (eV/A^2) */
+  double energy;     /* EAM energy at the final positions (eV) */
+} flygpu_search_result;
+
+/* Launch shape of the batched search kernel: lanes per atom in the EAM passes (1, 2, 4, 8),
+ * threads per CTA (multiple of 32) and resident CTAs per SM of the persistent grid. */
+typedef struct {
+  int lanes_per_atom, threads, blocks_per_sm, pad_;
+} flygpu_tuning;
+
+typedef struct flygpu_batch flygpu_batch;
+
+/* Master::find_batch's fan-out (saddle/find.cpp:684-732) as one persistent launch: every search of
+ * the batch is resident in HBM; one CTA runs one search at a time, largest first. */
+int flygpu_batch_create(flygpu_eam* eam, const flygpu_dimer_options* dimer, const flygpu_lbfgs_options* lbfgs,
+                        int precision, const flygpu_search_desc* descs, int n_search, void* stream,
+                        flygpu_batch** out);
+void flygpu_batch_destroy(flygpu_batch* batch);
+/* Runs every unfinished search to completion (asynchronous). tuning NULL = the autotuned shape. */
+int flygpu_batch_run(flygpu_batch* batch, const flygpu_tuning* tuning);
+/* Times candidate launch shapes on a sample of the batch's searches and returns the fastest; the
+ * choice is cached per (device, atoms-per-search bucket). Leaves the batch reset. */
+int flygpu_batch_autotune(flygpu_batch* batch, flygpu_tuning* best);
+/* Restores every search's inputs so the batch can run again. */
+int flygpu_batch_reset(flygpu_batch* batch);
+/* Waits for the batch and copies results; pos_out / axis_out (sum of 3n) may be NULL. */
+int flygpu_batch_results(flygpu_batch* batch, flygpu_search_result* results, double* pos_out, double* axis_out);
+int64_t flygpu_batch_device_bytes(const flygpu_batch* batch);
+
+/* Dimer::find_sp / LBFGS::minimise for one system the plain drop-in way: the search runs on the host
+ * (the reference's algorithm) and every gradient goes through this library's List and EAM on the GPU,
+ * one search at a time. */
+int flygpu_search_plain(flygpu_eam* eam, const flygpu_dimer_options* dimer, const flygpu_lbfgs_options* lbfgs,
+                        int precision, const flygpu_search_desc* desc, double* pos_out, double* axis_out,
+                        flygpu_search_result* result);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,857 @@
+// search.cu -- batched, resumable dimer searches and L-BFGS minimisations, one CTA per search.
+//
+// Device restatement of the reference's search stack for many independent searches at once:
+//   Dimer::find_sp        src/saddle/dimer.cpp:28-171
+//   Rotor::eff_gradient   src/saddle/rotor.cpp:49-164 (trans_proj rotor.cpp:33-47)
+//   StepLBFGS::newton_step src/minimise/LBFGS/lbfgs_core.cpp:29-87
+//   LBFGS::minimise       src/minimise/LBFGS/lbfgs.cpp:29-115
+//   EAM::gradient/energy  src/potential/EAM/eam.cpp:33-120 over a per-search neighbour list
+// A persistent grid pulls searches from an atomic work counter (largest first). The CTA owning a
+// search runs its control flow uniformly: every thread holds the same scalars, vectors are split
+// over threads by degree of freedom, and each dot product is one binary64 block reduction.
+// Vectors are compacted to mobile atoms (not frozen, or with a non-zero axis component): the
+// reference's vectors are exactly zero elsewhere, so the compacted algebra is the same algebra.
+// State lives in global memory (L2-resident while the search runs) and is saved at translation-step
+// boundaries, so a launch can stop after `budget` steps and a later launch resumes the search.
+// Kernels never trap and never wait on other CTAs: errors set the search's status and end it.
+
+#include "search.hpp"
+
+namespace flygpu {
+
+  namespace {
+
+    constexpr int MAXW = 32;
+
+    struct Blk {
+      double red[4 * MAXW];
+      double bc[4];
+      double rhoR[MAX_HIST], alphaR[MAX_HIST];
+      int item;
+      int flag;
+    };
+
+    enum : int { F_OOB = 1, F_NLIST = 2 };
+
+    __device__ inline double warp_sum(double v) {
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      return v;
+    }
+
+    // Sums K values over the block; every thread receives the totals.
+    template <int K>
+    __device__ inline void bsum(double (&v)[K], Blk& sh) {
+      int const lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+      for (int k = 0; k < K; ++k) v[k] = warp_sum(v[k]);
+      if (lane == 0) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) sh.red[w * K + k] = v[k];
+      }
+      __syncthreads();
+      if (w == 0) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+          double x = lane < nw ? sh.red[lane * K + k] : 0.0;
+          x = warp_sum(x);
+          if (lane == 0) sh.bc[k] = x;
+        }
+      }
+      __syncthreads();
+#pragma unroll
+      for (int k = 0; k < K; ++k) v[k] = sh.bc[k];
+    }
+
+    __device__ inline double dot1(double const* a, double const* b, int M, Blk& sh) {
+      double v[1] = {0.0};
+      for (int e = threadIdx.x; e < M; e += blockDim.x) v[0] += a[e] * b[e];
+      bsum<1>(v, sh);
+      return v[0];
+    }
+
+    struct Ctx {
+      SearchDev* S;
+      int n, na, M, mT, mR;
+      D4* xl;
+      Packed* pk;
+      std::uint8_t const* ty;
+      int const* aatom;
+      std::uint16_t* ncnt;
+      std::uint16_t* nbr;
+      double* v;
+      double const* hist;
+      double rc2;
+      float rc2f;
+      double L[3], invL[3];
+      float Lf[3];
+      bool per[3], periodic;
+      double shift[3];
+      __device__ double* V(int k) const { return v + static_cast<std::int64_t>(k) * M; }
+      __device__ double* sT(int j) const { return v + static_cast<std::int64_t>(N_VEC + j) * M; }
+      __device__ double* yT(int j) const { return v + static_cast<std::int64_t>(N_VEC + mT + j) * M; }
+      __device__ double* sR(int j) const { return v + static_cast<std::int64_t>(N_VEC + 2 * mT + j) * M; }
+      __device__ double* yR(int j) const { return v + static_cast<std::int64_t>(N_VEC + 2 * mT + mR + j) * M; }
+    };
+
+    __device__ inline double& comp(D4& p, int c) { return c == 0 ? p.x : c == 1 ? p.y : p.z; }
+
+    __device__ inline void pack_one(Ctx const& c, int a) {
+      D4 const p = c.xl[a];
+      double const X = p.x + c.shift[0], Y = p.y + c.shift[1], Z = p.z + c.shift[2];
+      Packed& q = c.pk[a];
+      float const hx = static_cast<float>(X), hy = static_cast<float>(Y), hz = static_cast<float>(Z);
+      q.hx = hx;
+      q.hy = hy;
+      q.hz = hz;
+      q.lx = static_cast<float>(X - static_cast<double>(hx));
+      q.ly = static_cast<float>(Y - static_cast<double>(hy));
+      q.lz = static_cast<float>(Z - static_cast<double>(hz));
+    }
+
+    // ------------------------------------------------------------------ pair geometry
+
+    __device__ inline void dr64(Ctx const& c, int i, int j, double& dx, double& dy, double& dz) {
+      D4 const a = c.xl[i], b = c.xl[j];
+      dx = b.x - a.x;
+      dy = b.y - a.y;
+      dz = b.z - a.z;
+      if (c.periodic) {
+        if (c.per[0]) dx -= c.L[0] * rint(dx * c.invL[0]);
+        if (c.per[1]) dy -= c.L[1] * rint(dy * c.invL[1]);
+        if (c.per[2]) dz -= c.L[2] * rint(dz * c.invL[2]);
+      }
+    }
+
+    __device__ inline void dr32(Ctx const& c, Packed const& me, int i, int j, float& dx, float& dy, float& dz) {
+      if (c.periodic) {
+        double a, b, d;
+        dr64(c, i, j, a, b, d);
+        dx = static_cast<float>(a);
+        dy = static_cast<float>(b);
+        dz = static_cast<float>(d);
+      } else {
+        Packed const o = c.pk[j];
+        dx = (o.hx - me.hx) + (o.lx - me.lx);
+        dy = (o.hy - me.hy) + (o.ly - me.ly);
+        dz = (o.hz - me.hz) + (o.lz - me.lz);
+      }
+    }
+
+    __device__ inline bool fetch64(double x, double inv_dx, double dx, int n, long long& i, double& x0) {
+      if (!(x >= 0)) return false;
+      double const u = x * inv_dx;
+      if (!(u < static_cast<double>(n))) return false;
+      i = static_cast<long long>(u);
+      x0 = x - static_cast<double>(i) * dx;
+      return true;
+    }
+
+    __device__ inline bool fetch32(float r, float inv_dx, int n, int& i, float& t) {
+      float const u = r * inv_dx;
+      if (!(u >= 0.f) || !(u < static_cast<float>(n))) return false;
+      i = static_cast<int>(u);
+      t = u - static_cast<float>(i);
+      return true;
+    }
+
+    template <int LPA>
+    __device__ inline double lane_sum(double v) {
+#pragma unroll
+      for (int o = LPA / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o, LPA);
+      return v;
+    }
+
+    // ------------------------------------------------------------------ EAM passes
+
+    // Density pass over all atoms: F'(rho) into xl[i].w (and pk[i].fp). With ENERGY, accumulates
+    // 0.5 * sum v + F(rho) into *e (per thread).
+    template <bool MIXED, int LPA, bool ENERGY>
+    __device__ void density(Ctx const& c, TablesView const& tb, Blk& sh, double* e) {
+      int const nt = blockDim.x;
+      int const total = c.n * LPA;
+      int const rounds = (total + nt - 1) / nt;
+      int const nty = tb.n_types;
+      for (int r = 0; r < rounds; ++r) {
+        int const t = r * nt + threadIdx.x;
+        bool const valid = t < total;
+        int const i = valid ? t / LPA : 0;
+        int const l = t % LPA;
+        double rho = 0, vs = 0;
+        if (valid) {
+          int const ti = c.ty[i];
+          int const cnt = c.ncnt[i];
+          if (MIXED) {
+            Packed const me = c.pk[i];
+            float rf = 0.f, vf = 0.f;
+            int chunk = 0;
+            for (int k = l; k < cnt; k += LPA) {
+              int const j = c.nbr[static_cast<std::int64_t>(k) * c.n + i];
+              float dx, dy, dz;
+              dr32(c, me, i, j, dx, dy, dz);
+              float const r2 = dx * dx + dy * dy + dz * dz;
+              if (r2 < c.rc2f) {
+                int const tj = c.ty[j];
+                int ii;
+                float tt;
+                if (!fetch32(sqrtf(r2), tb.finv_dR, tb.nR, ii, tt)) {
+                  atomicOr(&sh.flag, F_OOB);
+                  continue;
+                }
+                float4 const cp = __ldg(&tb.phi32[static_cast<std::int64_t>(tj + nty * ti) * tb.nR + ii]);
+                rf += cp.x + tt * (cp.y + tt * (cp.z + tt * cp.w));
+                if (ENERGY) {
+                  float4 const cv = __ldg(&tb.v32[static_cast<std::int64_t>(ti + nty * tj) * tb.nR + ii]);
+                  vf += cv.x + tt * (cv.y + tt * (cv.z + tt * cv.w));
+                }
+              }
+              if (++chunk == 8) {
+                rho += static_cast<double>(rf);
+                vs += static_cast<double>(vf);
+                rf = vf = 0.f;
+                chunk = 0;
+              }
+            }
+            rho += static_cast<double>(rf);
+            vs += static_cast<double>(vf);
+          } else {
+            for (int k = l; k < cnt; k += LPA) {
+              int const j = c.nbr[static_cast<std::int64_t>(k) * c.n + i];
+              double dx, dy, dz;
+              dr64(c, i, j, dx, dy, dz);
+              double const r2 = (dx * dx + dy * dy) + dz * dz;
+              if (r2 < c.rc2) {
+                int const tj = c.ty[j];
+                long long ii;
+                double x0;
+                if (!fetch64(sqrt(r2), tb.inv_dR, tb.dR, tb.nR, ii, x0)) {
+                  atomicOr(&sh.flag, F_OOB);
+                  continue;
+                }
+                D4 const cp = tb.phi64[static_cast<std::int64_t>(tj + nty * ti) * tb.nR + ii];
+                rho += cp.x + x0 * (cp.y + x0 * (cp.z + x0 * cp.w));
+                if (ENERGY) {
+                  D4 const cv = tb.v64[static_cast<std::int64_t>(ti + nty * tj) * tb.nR + ii];
+                  vs += cv.x + x0 * (cv.y + x0 * (cv.z + x0 * cv.w));
+                }
+              }
+            }
+          }
+        }
+        rho = lane_sum<LPA>(rho);
+        if (ENERGY) vs = lane_sum<LPA>(vs);
+        if (valid && l == 0) {
+          int const ti = c.ty[i];
+          long long ii;
+          double x0;
+          double fp = 0, fe = 0;
+          if (fetch64(rho, tb.inv_dP, tb.dP, tb.nP, ii, x0)) {
+            D4 const cf = tb.F64[static_cast<std::int64_t>(ti) * tb.nP + ii];
+            fp = cf.y + x0 * (2.0 * cf.z + x0 * 3.0 * cf.w);
+            if (ENERGY) fe = cf.x + x0 * (cf.y + x0 * (cf.z + x0 * cf.w));
+          } else {
+            atomicOr(&sh.flag, F_OOB);
+          }
+          c.xl[i].w = fp;
+          if (MIXED) c.pk[i].fp = static_cast<float>(fp);
+          if (ENERGY) *e += 0.5 * vs + fe;
+        }
+      }
+    }
+
+    // Force pass over mobile atoms into out (3 per mobile atom).
+    template <bool MIXED, int LPA>
+    __device__ void force(Ctx const& c, TablesView const& tb, Blk& sh, double* out) {
+      int const nt = blockDim.x;
+      int const total = c.na * LPA;
+      int const rounds = (total + nt - 1) / nt;
+      int const nty = tb.n_types;
+      for (int r = 0; r < rounds; ++r) {
+        int const t = r * nt + threadIdx.x;
+        bool const valid = t < total;
+        int const k0 = valid ? t / LPA : 0;
+        int const l = t % LPA;
+        int const i = valid ? c.aatom[k0] : 0;
+        double gx = 0, gy = 0, gz = 0;
+        if (valid) {
+          int const ti = c.ty[i];
+          int const cnt = c.ncnt[i];
+          if (MIXED) {
+            Packed const me = c.pk[i];
+            float fx = 0.f, fy = 0.f, fz = 0.f;
+            int chunk = 0;
+            float const inv = tb.finv_dR;
+            for (int k = l; k < cnt; k += LPA) {
+              int const j = c.nbr[static_cast<std::int64_t>(k) * c.n + i];
+              float dx, dy, dz;
+              dr32(c, me, i, j, dx, dy, dz);
+              float const r2 = dx * dx + dy * dy + dz * dz;
+              if (r2 < c.rc2f) {
+                float const ir = rsqrtf(r2);
+                int const tj = c.ty[j];
+                int ii;
+                float tt;
+                if (!fetch32(r2 * ir, inv, tb.nR, ii, tt)) {
+                  atomicOr(&sh.flag, F_OOB);
+                  continue;
+                }
+                float4 const cv = __ldg(&tb.v32[static_cast<std::int64_t>(tj + nty * ti) * tb.nR + ii]);
+                float4 const ca = __ldg(&tb.phi32[static_cast<std::int64_t>(tj + nty * ti) * tb.nR + ii]);
+                float4 const cb = __ldg(&tb.phi32[static_cast<std::int64_t>(ti + nty * tj) * tb.nR + ii]);
+                float const dv = cv.y + tt * (2.f * cv.z + 3.f * tt * cv.w);
+                float const da = ca.y + tt * (2.f * ca.z + 3.f * tt * ca.w);
+                float const db = cb.y + tt * (2.f * cb.z + 3.f * tt * cb.w);
+                float const fpj = c.pk[j].fp;
+                float const s = (dv + me.fp * da + fpj * db) * inv * ir;
+                fx -= s * dx;
+                fy -= s * dy;
+                fz -= s * dz;
+              }
+              if (++chunk == 8) {
+                gx += static_cast<double>(fx);
+                gy += static_cast<double>(fy);
+                gz += static_cast<double>(fz);
+                fx = fy = fz = 0.f;
+                chunk = 0;
+              }
+            }
+            gx += static_cast<double>(fx);
+            gy += static_cast<double>(fy);
+            gz += static_cast<double>(fz);
+          } else {
+            double const fpi = c.xl[i].w;
+            for (int k = l; k < cnt; k += LPA) {
+              int const j = c.nbr[static_cast<std::int64_t>(k) * c.n + i];
+              double dx, dy, dz;
+              dr64(c, i, j, dx, dy, dz);
+              double const r2 = (dx * dx + dy * dy) + dz * dz;
+              if (r2 < c.rc2) {
+                double const r = sqrt(r2);
+                int const tj = c.ty[j];
+                long long ii;
+                double x0;
+                if (!fetch64(r, tb.inv_dR, tb.dR, tb.nR, ii, x0)) {
+                  atomicOr(&sh.flag, F_OOB);
+                  continue;
+                }
+                D4 const cv = tb.v64[static_cast<std::int64_t>(tj + nty * ti) * tb.nR + ii];
+                D4 const ca = tb.phi64[static_cast<std::int64_t>(tj + nty * ti) * tb.nR + ii];
+                D4 const cb = tb.phi64[static_cast<std::int64_t>(ti + nty * tj) * tb.nR + ii];
+                double const mag = (cv.y + x0 * (2.0 * cv.z + x0 * 3.0 * cv.w)) +
+                                   fpi * (ca.y + x0 * (2.0 * ca.z + x0 * 3.0 * ca.w)) +
+                                   c.xl[j].w * (cb.y + x0 * (2.0 * cb.z + x0 * 3.0 * cb.w));
+                double const s = mag / r;
+                gx -= s * dx;
+                gy -= s * dy;
+                gz -= s * dz;
+              }
+            }
+          }
+        }
+        gx = lane_sum<LPA>(gx);
+        gy = lane_sum<LPA>(gy);
+        gz = lane_sum<LPA>(gz);
+        if (valid && l == 0) {
+          out[3 * k0 + 0] = gx;
+          out[3 * k0 + 1] = gy;
+          out[3 * k0 + 2] = gz;
+        }
+      }
+    }
+
+    template <bool MIXED, int LPA>
+    __device__ void gradient(Ctx const& c, TablesView const& tb, Blk& sh, double* out) {
+      __syncthreads();
+      if (MIXED) {
+        for (int k = threadIdx.x; k < c.na; k += blockDim.x) pack_one(c, c.aatom[k]);
+        __syncthreads();
+      }
+      density<MIXED, LPA, false>(c, tb, sh, nullptr);
+      __syncthreads();
+      force<MIXED, LPA>(c, tb, sh, out);
+      __syncthreads();
+      if (threadIdx.x == 0) c.S->grad_calls += 1;
+    }
+
+    template <bool MIXED, int LPA>
+    __device__ double energy(Ctx const& c, TablesView const& tb, Blk& sh) {
+      __syncthreads();
+      if (MIXED) {
+        for (int k = threadIdx.x; k < c.na; k += blockDim.x) pack_one(c, c.aatom[k]);
+        __syncthreads();
+      }
+      double e[1] = {0.0};
+      density<MIXED, LPA, true>(c, tb, sh, &e[0]);
+      bsum<1>(e, sh);
+      return e[0];
+    }
+
+    // ------------------------------------------------------------------ neighbour list
+
+    // List::update (list.cpp:37-51) on mobile atoms: xl -= d.
+    __device__ inline void list_update(Ctx const& c, double const* d) {
+      for (int e = threadIdx.x; e < c.M; e += blockDim.x) comp(c.xl[c.aatom[e / 3]], e % 3) -= d[e];
+    }
+
+    // List::rebuild (list.cpp:53-95): canonical images of the mobile positions, then every pair within
+    // rc_list (plus a margin covering binary32 rounding) -- a superset of the reference's list, so the
+    // exact r < r_cut filter at evaluation time sees the same pairs.
+    __device__ void rebuild(Ctx const& c, Blk& sh, double rc_list) {
+      double const* X = c.V(V_X);
+      for (int e = threadIdx.x; e < c.M; e += blockDim.x) {
+        int const k = e % 3;
+        comp(c.xl[c.aatom[e / 3]], k) = X[e] - c.L[k] * floor(X[e] * c.invL[k]);
+      }
+      __syncthreads();
+      for (int k = threadIdx.x; k < c.na; k += blockDim.x) pack_one(c, c.aatom[k]);
+      __syncthreads();
+      float const lim = static_cast<float>((rc_list + 1e-3) * (rc_list + 1e-3));
+      for (int i = threadIdx.x; i < c.n; i += blockDim.x) {
+        Packed const me = c.pk[i];
+        int cnt = 0;
+        for (int j = 0; j < c.n; ++j) {
+          Packed const o = c.pk[j];
+          float dx = o.hx - me.hx, dy = o.hy - me.hy, dz = o.hz - me.hz;
+          if (c.periodic) {
+            if (c.per[0]) dx -= c.Lf[0] * rintf(dx / c.Lf[0]);
+            if (c.per[1]) dy -= c.Lf[1] * rintf(dy / c.Lf[1]);
+            if (c.per[2]) dz -= c.Lf[2] * rintf(dz / c.Lf[2]);
+          }
+          if (j != i && dx * dx + dy * dy + dz * dz < lim) {
+            if (cnt < NB_CAP) c.nbr[static_cast<std::int64_t>(cnt) * c.n + i] = static_cast<std::uint16_t>(j);
+            ++cnt;
+          }
+        }
+        if (cnt > NB_CAP) atomicOr(&sh.flag, F_NLIST);
+        c.ncnt[i] = static_cast<std::uint16_t>(min(cnt, NB_CAP));
+      }
+      __syncthreads();
+    }
+
+    // ------------------------------------------------------------------ L-BFGS two-loop core
+
+    // StepLBFGS::newton_step_impl (lbfgs_core.cpp:29-87) over the block's vectors.
+    // s(j) = s0 + j M and y(j) = y0 + j M hold the history; rho / alpha its scalars.
+    __device__ void newton(Ctx const& c, Blk& sh, int m, int& k, double* s0, double* y0, double* rho, double* alpha,
+                           double* px, double* pg, double const* x, double const* g, double* out) {
+      int const M = c.M;
+      auto S_ = [&](int j) { return s0 + static_cast<std::int64_t>(j) * M; };
+      auto Y_ = [&](int j) { return y0 + static_cast<std::int64_t>(j) * M; };
+      int const prev = k > 0 ? (k - 1) % m : 0;
+      if (k > 0) {
+        double* sp = S_(prev);
+        double* yp = Y_(prev);
+        double d[1] = {0.0};
+        for (int e = threadIdx.x; e < M; e += blockDim.x) {
+          sp[e] = x[e] - px[e];
+          yp[e] = g[e] - pg[e];
+          d[0] += sp[e] * yp[e];
+        }
+        bsum<1>(d, sh);
+        if (threadIdx.x == 0) rho[prev] = 1.0 / fabs(d[0]);
+      }
+      for (int e = threadIdx.x; e < M; e += blockDim.x) {
+        px[e] = x[e];
+        pg[e] = g[e];
+        out[e] = g[e];
+      }
+      int const incur = k <= m ? 0 : k - m;
+      int const bound = k <= m ? k : m;
+      for (int i = bound - 1; i >= 0; --i) {
+        int const j = (i + incur) % m;
+        double const* s = S_(j);
+        double const* y = Y_(j);
+        double d[1] = {0.0};
+        for (int e = threadIdx.x; e < M; e += blockDim.x) d[0] += s[e] * out[e];
+        bsum<1>(d, sh);
+        double const a = rho[j] * d[0];
+        if (threadIdx.x == 0) alpha[j] = a;
+        for (int e = threadIdx.x; e < M; e += blockDim.x) out[e] -= a * y[e];
+      }
+      if (k > 0) {
+        double const* yp = Y_(prev);
+        double const yy = dot1(yp, yp, M, sh);
+        double const scale = 1.0 / rho[prev] / yy;
+        for (int e = threadIdx.x; e < M; e += blockDim.x) out[e] = out[e] * scale;
+      }
+      for (int i = 0; i <= bound - 1; ++i) {
+        int const j = (i + incur) % m;
+        double const* s = S_(j);
+        double const* y = Y_(j);
+        double d[1] = {0.0};
+        for (int e = threadIdx.x; e < M; e += blockDim.x) d[0] += y[e] * out[e];
+        bsum<1>(d, sh);
+        double const beta = rho[j] * d[0];
+        double const a = alpha[j];
+        for (int e = threadIdx.x; e < M; e += blockDim.x) out[e] += (a - beta) * s[e];
+      }
+      ++k;
+    }
+
+    // trans_proj (rotor.cpp:33-47): remove the mean per component.
+    __device__ void trans_proj(Ctx const& c, Blk& sh, double* x) {
+      double p[3] = {0.0, 0.0, 0.0};
+      for (int e = threadIdx.x; e < c.M; e += blockDim.x) p[e % 3] += x[e];
+      bsum<3>(p, sh);
+      double const inv = 1.0 / static_cast<double>(c.na);
+      double const q[3] = {p[0] * inv, p[1] * inv, p[2] * inv};
+      for (int e = threadIdx.x; e < c.M; e += blockDim.x) x[e] -= q[e % 3];
+    }
+
+    // ------------------------------------------------------------------ Rotor::eff_gradient
+
+    template <bool MIXED, int LPA>
+    __device__ double eff_gradient(Ctx const& c, TablesView const& tb, SearchOpts const& o, Blk& sh) {
+      int const M = c.M;
+      double* ax = c.V(V_AX);
+      double* g0 = c.V(V_G0);
+      double* g1 = c.V(V_G1);
+      double* g1p = c.V(V_G1P);
+      double* dprev = c.V(V_DPREV);
+      double* axp = c.V(V_AXP);
+      double* th = c.V(V_TH);
+      double* eff = c.V(V_EFF);
+      double const dr = o.delta_r;
+      int kR = 0;
+      gradient<MIXED, LPA>(c, tb, sh, g0);
+      for (int e = threadIdx.x; e < M; e += blockDim.x) dprev[e] = -dr * ax[e];
+      list_update(c, dprev);
+      gradient<MIXED, LPA>(c, tb, sh, g1);
+      double curv = 0;
+      for (int i = 0;; i++) {
+        double* dg = g1p;  // scratch until the trial gradient is evaluated
+        double t[1] = {0.0};
+        for (int e = threadIdx.x; e < M; e += blockDim.x) {
+          dg[e] = g1[e] - g0[e];
+          t[0] += dg[e] * ax[e];
+        }
+        bsum<1>(t, sh);
+        for (int e = threadIdx.x; e < M; e += blockDim.x) dg[e] -= t[0] * ax[e];
+        if (c.S->count_frozen == 0) trans_proj(c, sh, dg);
+        newton(c, sh, c.mR, kR, c.sR(0), c.yR(0), sh.rhoR, sh.alphaR, c.V(V_PXR), c.V(V_PGR), ax, dg, th);
+        double const tp = dot1(th, ax, M, sh);
+        double nn[1] = {0.0};
+        for (int e = threadIdx.x; e < M; e += blockDim.x) {
+          th[e] -= tp * ax[e];
+          nn[0] += th[e] * th[e];
+        }
+        bsum<1>(nn, sh);
+        double const inv = 1 / sqrt(nn[0]);
+        double bc[2] = {0.0, 0.0};
+        for (int e = threadIdx.x; e < M; e += blockDim.x) {
+          th[e] *= inv;
+          double const df = g1[e] - g0[e];
+          bc[0] += df * th[e];
+          bc[1] += df * ax[e];
+        }
+        bsum<2>(bc, sh);
+        double const b_1 = bc[0] / dr;
+        double const c_x0 = bc[1] / dr;
+        double const theta_1 = -0.5 * atan(b_1 / fabs(c_x0));
+        if (fabs(theta_1) < o.theta_tol || (i >= o.iter_max_rot && c_x0 < 0) || i > 10 * o.iter_max_rot) {
+          curv = c_x0;
+          break;
+        }
+        double const c1 = cos(theta_1), s1 = sin(theta_1);
+        for (int e = threadIdx.x; e < M; e += blockDim.x) {
+          axp[e] = ax[e] * c1 + th[e] * s1;
+          double const nd = -dr * axp[e];
+          double const upd = nd - dprev[e];
+          dprev[e] = nd;
+          comp(c.xl[c.aatom[e / 3]], e % 3) -= upd;
+        }
+        gradient<MIXED, LPA>(c, tb, sh, g1p);
+        double cx[1] = {0.0};
+        for (int e = threadIdx.x; e < M; e += blockDim.x) cx[0] += (g1p[e] - g0[e]) * axp[e];
+        bsum<1>(cx, sh);
+        double const c_x1 = cx[0] / dr;
+        double const a_1 = (c_x0 - c_x1 + b_1 * sin(2 * theta_1)) / (1 - cos(2 * theta_1));
+        double theta_min = 0.5 * atan(b_1 / a_1);
+        if (a_1 * cos(2 * theta_min) - a_1 + b_1 * sin(2 * theta_min) > 0) theta_min += M_PI / 2;
+        double const cm = cos(theta_min), sm = sin(theta_min);
+        double const w1 = sin(theta_1 - theta_min) / sin(theta_1);
+        double const w1p = sm / sin(theta_1);
+        double const w0 = 1 - cm - sm * tan(0.5 * theta_1);
+        for (int e = threadIdx.x; e < M; e += blockDim.x) {
+          ax[e] = ax[e] * cm + th[e] * sm;
+          g1[e] = w1 * g1[e] + w1p * g1p[e] + w0 * g0[e];
+        }
+        if (fabs(theta_min) < o.theta_tol) {
+          double q[1] = {0.0};
+          for (int e = threadIdx.x; e < M; e += blockDim.x) q[0] += (g1[e] - g0[e]) * ax[e];
+          bsum<1>(q, sh);
+          curv = q[0] / dr;
+          break;
+        }
+      }
+      for (int e = threadIdx.x; e < M; e += blockDim.x) comp(c.xl[c.aatom[e / 3]], e % 3) -= -dprev[e];
+      double const p = dot1(g0, ax, M, sh);
+      bool const parallel_only = !o.relax_in_convex && curv > 0;
+      for (int e = threadIdx.x; e < M; e += blockDim.x) eff[e] = parallel_only ? -p * ax[e] : g0[e] - 2 * p * ax[e];
+      if (c.S->count_frozen == 0) trans_proj(c, sh, eff);
+      __syncthreads();
+      return curv;
+    }
+
+    // ------------------------------------------------------------------ one search
+
+    template <bool MIXED, int LPA>
+    __device__ void run(BatchView const& bv, Blk& sh, int sidx) {
+      SearchDev* S = bv.S + sidx;
+      if (S->stage == STAGE_DONE) return;
+      SearchOpts const& o = bv.o;
+      Ctx c;
+      c.S = S;
+      c.n = S->n;
+      c.na = S->na;
+      c.M = 3 * S->na;
+      bool const dimer = S->mode == MODE_DIMER;
+      c.mT = dimer ? o.mT : o.mL;
+      c.mR = dimer ? o.mR : 0;
+      c.xl = bv.xl + S->atom_off;
+      c.pk = bv.pk + S->atom_off;
+      c.ty = bv.type + S->atom_off;
+      c.aatom = bv.aatom + S->act_off;
+      c.ncnt = bv.ncnt + S->atom_off;
+      c.nbr = bv.nbr + S->atom_off * NB_CAP;
+      c.v = bv.vec + S->vec_off;
+      c.hist = bv.hist + S->hist_off;
+      c.rc2 = o.r_cut * o.r_cut;
+      c.rc2f = static_cast<float>(c.rc2);
+      c.periodic = S->periodic_any != 0;
+      for (int k = 0; k < 3; ++k) {
+        c.L[k] = S->L[k];
+        c.invL[k] = 1.0 / S->L[k];
+        c.Lf[k] = static_cast<float>(S->L[k]);
+        c.per[k] = S->per[k] != 0;
+        c.shift[k] = S->shift[k];
+      }
+      TablesView const& tb = bv.tb;
+      double const skin = S->rc_list - (dimer ? o.r_cut + 2 * o.delta_r : o.r_cut);
+      double* X = c.V(V_X);
+      double* eff = c.V(V_EFF);
+      double* hg = c.V(V_HG);
+      int const M = c.M;
+      if (threadIdx.x == 0) sh.flag = 0;
+      __syncthreads();
+
+      int kT = S->kT, it = S->it;
+      double trust = S->trust, acc = S->acc, convex = S->convex, curv = S->curv;
+      int exit_code = FLYGPU_EXIT_UNINIT;
+      bool done = false;
+
+      auto failed = [&]() -> bool {
+        __syncthreads();
+        int const f = sh.flag;
+        __syncthreads();
+        if (f) {
+          if (threadIdx.x == 0) S->status = (f & F_NLIST) ? FLYGPU_NLIST_OVERFLOW : FLYGPU_SPLINE_OOB;
+          done = true;
+        }
+        return f != 0;
+      };
+
+      if (S->stage == STAGE_INIT) {
+        for (int i = threadIdx.x; i < c.n; i += blockDim.x) {
+          D4& p = c.xl[i];
+          p.x = p.x - c.L[0] * floor(p.x * c.invL[0]);
+          p.y = p.y - c.L[1] * floor(p.y * c.invL[1]);
+          p.z = p.z - c.L[2] * floor(p.z * c.invL[2]);
+          pack_one(c, i);
+        }
+        __syncthreads();
+        rebuild(c, sh, S->rc_list);
+        kT = 0;
+        it = 0;
+        acc = 0;
+        convex = 0;
+        curv = 0;
+        if (!failed()) {
+          if (dimer) {
+            curv = eff_gradient<MIXED, LPA>(c, tb, o, sh);
+            trust = o.min_trust;
+          } else {
+            gradient<MIXED, LPA>(c, tb, sh, eff);
+            trust = o.min_trust_l;
+          }
+          failed();
+        }
+      }
+
+      int const max_steps = dimer ? o.max_steps : o.iter_max_l;
+      double const f2 = dimer ? o.f2norm : o.f2norm_l;
+      int steps_here = 0;
+      while (!done) {
+        if (it >= max_steps) {
+          exit_code = dimer ? FLYGPU_EXIT_ITER_MAX : 1;
+          done = true;
+          break;
+        }
+        if (bv.budget > 0 && steps_here >= bv.budget) break;
+        double const mag = dot1(eff, eff, M, sh);
+        if (mag < f2 * f2) {
+          exit_code = dimer ? FLYGPU_EXIT_SUCCESS : 0;
+          done = true;
+          break;
+        }
+        if (dimer && convex >= o.convex_max) {
+          exit_code = FLYGPU_EXIT_CONVEX;
+          done = true;
+          break;
+        }
+        if (dimer && o.use_history && S->n_hist > 0 && it % o.hist_check_freq == 0) {
+          double ctheta = -1;
+          double const* im = c.V(V_INMIN);
+          bool hit = false;
+          for (int h = 0; h < S->n_hist; ++h) {
+            double const* sp = c.hist + static_cast<std::int64_t>(h) * M;
+            double q[3] = {0.0, 0.0, 0.0};
+            for (int e = threadIdx.x; e < M; e += blockDim.x) {
+              double const d1 = X[e] - im[e], d2 = sp[e] - im[e];
+              q[0] += d1 * d2;
+              q[1] += d2 * d2;
+              q[2] += d1 * d1;
+            }
+            bsum<3>(q, sh);
+            ctheta = fmax(ctheta, q[0] / (sqrt(q[1]) * sqrt(q[2])));
+            if (ctheta > cos(S->theta_tol_hist)) {
+              hit = true;
+              break;
+            }
+          }
+          if (hit) {
+            exit_code = FLYGPU_EXIT_COLLISION;
+            done = true;
+            break;
+          }
+        }
+        newton(c, sh, c.mT, kT, c.sT(0), c.yT(0), S->rhoT, S->alphaT, c.V(V_PXT), c.V(V_PGT), X, eff, hg);
+        double const nrm = dot1(hg, hg, M, sh);
+        double const sc = fmin(1.0, trust / sqrt(nrm));
+        double hh[1] = {0.0};
+        for (int e = threadIdx.x; e < M; e += blockDim.x) {
+          hg[e] *= sc;
+          hh[0] += hg[e] * hg[e];
+          X[e] -= hg[e];
+        }
+        bsum<1>(hh, sh);
+        acc += sqrt(hh[0]);
+        if (acc > 0.5 * skin) {
+          rebuild(c, sh, S->rc_list);
+          acc = 0;
+          if (failed()) break;
+        } else {
+          list_update(c, hg);
+        }
+        if (dimer) {
+          curv = eff_gradient<MIXED, LPA>(c, tb, o, sh);
+          convex = curv > 0 ? convex + 1 : 0;
+        } else {
+          gradient<MIXED, LPA>(c, tb, sh, eff);
+        }
+        if (failed()) break;
+        double const proj = dot1(eff, hg, M, sh);
+        double const ptol = dimer ? o.proj_tol : o.proj_tol_l;
+        if (proj < -ptol) {
+          trust = fmax(dimer ? o.min_trust : o.min_trust_l, (dimer ? o.shrink_trust : o.shrink_trust_l) * trust);
+        } else if (proj > ptol) {
+          trust = fmin(dimer ? o.max_trust : o.max_trust_l, (dimer ? o.grow_trust : o.grow_trust_l) * trust);
+        }
+        ++it;
+        ++steps_here;
+      }
+      double e_final = 0;
+      if (done && S->status == FLYGPU_OK) e_final = energy<MIXED, LPA>(c, tb, sh);
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        S->kT = kT;
+        S->it = it;
+        S->trust = trust;
+        S->acc = acc;
+        S->convex = convex;
+        S->curv = curv;
+        if (done) {
+          S->stage = STAGE_DONE;
+          S->exit_code = exit_code;
+          S->energy = e_final;
+        } else {
+          S->stage = STAGE_LOOP;
+        }
+      }
+      __syncthreads();
+    }
+
+    template <bool MIXED, int LPA>
+    __global__ void k_search(BatchView bv) {
+      __shared__ Blk sh;
+      for (;;) {
+        if (threadIdx.x == 0) sh.item = atomicAdd(bv.work, 1);
+        __syncthreads();
+        int const item = sh.item;
+        __syncthreads();
+        if (item >= bv.n_items) break;
+        run<MIXED, LPA>(bv, sh, bv.order[item]);
+      }
+    }
+
+    template <bool MIXED>
+    void launch_lpa(BatchView const& v, int lpa, int threads, int blocks, cudaStream_t s) {
+      switch (lpa) {
+        case 1: launch(k_search<MIXED, 1>, blocks, threads, 0, s, v); break;
+        case 2: launch(k_search<MIXED, 2>, blocks, threads, 0, s, v); break;
+        case 4: launch(k_search<MIXED, 4>, blocks, threads, 0, s, v); break;
+        case 8: launch(k_search<MIXED, 8>, blocks, threads, 0, s, v); break;
+        default: fail(FLYGPU_INVALID_ARG, "lanes per atom must be 1, 2, 4 or 8");
+      }
+    }
+
+    // Mobile positions and axes of every search into compact arrays (3 per mobile atom, batch order).
+    __global__ void k_gather_out(BatchView bv, std::int64_t const* __restrict__ act3, double* __restrict__ ox,
+                                 double* __restrict__ oa) {
+      int const s = blockIdx.x;
+      if (s >= bv.n_search) return;
+      SearchDev const& S = bv.S[s];
+      int const M = 3 * S.na;
+      double const* v = bv.vec + S.vec_off;
+      std::int64_t const o = act3[s];
+      for (int e = threadIdx.x; e < M; e += blockDim.x) {
+        ox[o + e] = v[static_cast<std::int64_t>(V_X) * M + e];
+        oa[o + e] = S.mode == MODE_DIMER ? v[static_cast<std::int64_t>(V_AX) * M + e] : 0.0;
+      }
+    }
+
+    template <bool MIXED>
+    void occupancy_lpa(int lpa, int threads, int* bps) {
+      switch (lpa) {
+        case 1: FLY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, k_search<MIXED, 1>, threads, 0)); break;
+        case 2: FLY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, k_search<MIXED, 2>, threads, 0)); break;
+        case 4: FLY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, k_search<MIXED, 4>, threads, 0)); break;
+        case 8: FLY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, k_search<MIXED, 8>, threads, 0)); break;
+        default: fail(FLYGPU_INVALID_ARG, "lanes per atom must be 1, 2, 4 or 8");
+      }
+    }
+
+  }  // namespace
+
+  void search_gather(BatchView const& v, std::int64_t const* d_act3_off, double* out_x, double* out_ax,
+                     cudaStream_t s) {
+    launch(k_gather_out, v.n_search, 128, 0, s, v, d_act3_off, out_x, out_ax);
+  }
+
+  void search_occupancy(int lanes_per_atom, int threads, bool mixed, int* blocks_per_sm) {
+    if (mixed) {
+      occupancy_lpa<true>(lanes_per_atom, threads, blocks_per_sm);
+    } else {
+      occupancy_lpa<false>(lanes_per_atom, threads, blocks_per_sm);
+    }
+  }
+
+  void search_launch(BatchView const& v, int lanes_per_atom, int threads, int blocks, bool mixed, cudaStream_t s) {
+    if (threads % 32 != 0 || threads < 32 || threads > 1024) fail(FLYGPU_INVALID_ARG, "threads must be 32..1024, multiple of 32");
+    if (mixed) {
+      launch_lpa<true>(v, lanes_per_atom, threads, blocks, s);
+    } else {
+      launch_lpa<false>(v, lanes_per_atom, threads, blocks, s);
+    }
+  }
+
+}  // namespace flygpu

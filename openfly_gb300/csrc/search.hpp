@@ -1,0 +1,89 @@
+// search.hpp -- device data layout of batched, resumable dimer searches and L-BFGS minimisations.
+#pragma once
+
+#include <cstdint>
+
+#include "internal.hpp"
+
+namespace flygpu {
+
+  constexpr int NB_CAP = 96;       // neighbour capacity per atom inside a search (uint16 local indices)
+  constexpr int MAX_ATOMS = 4096;  // atoms per search (local indices fit in uint16 with room to spare)
+  constexpr int MAX_HIST = 8;      // L-BFGS history length supported on the device
+  constexpr int N_VEC = 15;        // fixed per-DOF vectors of a search (see Vec below)
+
+  enum Mode : int { MODE_DIMER = 0, MODE_MINIMISE = 1 };
+  enum Stage : int { STAGE_INIT = 0, STAGE_LOOP = 1, STAGE_DONE = 2 };
+
+  // Per-DOF vectors (3 doubles per mobile atom), in this order inside a search's vector block.
+  enum Vec : int {
+    V_X = 0,      // dimer / minimiser positions of mobile atoms (Position)
+    V_AX,         // dimer axis (Axis)
+    V_EFF,        // effective gradient (dimer) or gradient (minimiser)
+    V_G0,         // rotor: gradient at the centre
+    V_G1,         // rotor: gradient at the end
+    V_G1P,        // rotor: gradient at the trial end
+    V_DPREV,      // rotor: displacement currently applied to the list
+    V_AXP,        // rotor: trial axis
+    V_TH,         // rotor L-BFGS output (rotation plane)
+    V_HG,         // translation L-BFGS output (step)
+    V_PXT, V_PGT, // translation L-BFGS previous x / g
+    V_PXR, V_PGR, // rotation L-BFGS previous x / g
+    V_INMIN,      // minimum the dimer climbs from (history check)
+  };
+
+  // Options shared by every search of a batch (Dimer::Options dimer.hpp:56-98, Rotor::Options
+  // rotor.hpp:47-60, LBFGS::Options lbfgs.hpp:56-80).
+  struct SearchOpts {
+    int mT, max_steps, hist_check_freq, use_history;
+    double f2norm, skin_frac, proj_tol, max_trust, min_trust, grow_trust, shrink_trust, convex_max;
+    int mR, iter_max_rot, relax_in_convex;
+    double delta_r, theta_tol;
+    // L-BFGS minimiser
+    int mL, iter_max_l;
+    double f2norm_l, skin_frac_l, proj_tol_l, max_trust_l, min_trust_l, grow_trust_l, shrink_trust_l;
+    double r_cut;  // potential cut-off
+  };
+
+  // One search: geometry, offsets into the batch arrays, resumable scalar state and results.
+  struct SearchDev {
+    int n, na, mode, count_frozen;
+    int n_hist, stage, it, kT;
+    int exit_code, status, pad0, pad1;
+    double L[3];
+    int per[3], periodic_any;
+    double shift[3];        // binary32 packed-coordinate offset per axis
+    double rc_list;         // neighbour-list cut-off of this search
+    double theta_tol_hist;  // collision angle (Master::find_batch, find.cpp:692)
+    std::int64_t atom_off, act_off, vec_off, hist_off;
+    double trust, acc, convex, curv, energy;
+    std::int64_t grad_calls;
+    double rhoT[MAX_HIST], alphaT[MAX_HIST];
+  };
+
+  struct BatchView {
+    SearchDev* S;
+    int n_search;
+    int const* order;         // work items -> search index
+    int n_items;
+    int* work;                // atomic work counter
+    int budget;               // translation steps per launch (<= 0: run to completion)
+    SearchOpts o;
+    TablesView tb;
+    D4* xl;                   // list positions per atom (w = F')
+    Packed* pk;               // binary32 records per atom
+    std::uint8_t* type;       // per atom
+    int* aidx;                // per atom: mobile index or -1
+    int* aatom;               // per mobile atom: local atom index
+    std::uint16_t* ncnt;      // per atom
+    std::uint16_t* nbr;       // [NB_CAP][n] per search, at atom_off * NB_CAP
+    double* vec;              // per search: (N_VEC + 2 mT + 2 mR) vectors of 3 na doubles
+    double const* hist;       // per search: n_hist vectors of 3 na doubles (previous saddle points)
+    int* err;                 // batch error word
+  };
+
+  // search.cu
+  void search_launch(BatchView const& v, int lanes_per_atom, int threads, int blocks, bool mixed, cudaStream_t s);
+  void search_occupancy(int lanes_per_atom, int threads, bool mixed, int* blocks_per_sm);
+
+}  // namespace flygpu

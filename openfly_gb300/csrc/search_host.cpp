@@ -1,0 +1,550 @@
+// search_host.cpp -- host side of batched searches: layout, launch, autotuning, results.
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <numeric>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "search.hpp"
+
+namespace flygpu {
+
+  void search_gather(BatchView const& v, std::int64_t const* d_act3_off, double* out_x, double* out_ax,
+                     cudaStream_t s);
+
+  // Options as the device sees them (all searches of a batch share them).
+  SearchOpts make_opts(flygpu_dimer_options const& d, flygpu_lbfgs_options const& l, double r_cut) {
+    SearchOpts o{};
+    o.mT = d.n;
+    o.max_steps = d.max_steps;
+    o.hist_check_freq = d.hist_check_freq;
+    o.use_history = d.use_history;
+    o.f2norm = d.f2norm;
+    o.skin_frac = d.skin_frac;
+    o.proj_tol = d.proj_tol;
+    o.max_trust = d.max_trust;
+    o.min_trust = d.min_trust;
+    o.grow_trust = d.grow_trust;
+    o.shrink_trust = d.shrink_trust;
+    o.convex_max = d.convex_max;
+    o.mR = d.rot_n;
+    o.iter_max_rot = d.iter_max_rot;
+    o.relax_in_convex = d.relax_in_convex;
+    o.delta_r = d.delta_r;
+    o.theta_tol = d.theta_tol;
+    o.mL = l.n;
+    o.iter_max_l = l.iter_max;
+    o.f2norm_l = l.f2norm;
+    o.skin_frac_l = l.skin_frac;
+    o.proj_tol_l = l.proj_tol;
+    o.max_trust_l = l.max_trust;
+    o.min_trust_l = l.min_trust;
+    o.grow_trust_l = l.grow_trust;
+    o.shrink_trust_l = l.shrink_trust;
+    o.r_cut = r_cut;
+    if (o.mT < 1 || o.mT > MAX_HIST || o.mR < 1 || o.mR > MAX_HIST || o.mL < 1 || o.mL > MAX_HIST)
+      fail(FLYGPU_INVALID_ARG, "L-BFGS history lengths must be 1..8 on the device");
+    if (o.max_steps < 0 || o.iter_max_l < 0 || o.hist_check_freq < 1) fail(FLYGPU_INVALID_ARG, "bad iteration limits");
+    return o;
+  }
+
+  // List cut-offs: Dimer::find_sp (dimer.cpp:47,53) and LBFGS::minimise (lbfgs.cpp:41-45).
+  double dimer_rc_list(SearchOpts const& o) {
+    double const rr = o.r_cut + o.delta_r * 2;
+    return rr + std::max(std::pow(o.skin_frac, 1. / 3.) - 1, 0.0) * rr;
+  }
+  double lbfgs_rc_list(SearchOpts const& o) {
+    return o.r_cut + std::max(std::pow(o.skin_frac_l, 1. / 3.) - 1, 0.0) * o.r_cut;
+  }
+
+}  // namespace flygpu
+
+using namespace flygpu;
+
+struct flygpu_batch {
+  flygpu_eam* eam = nullptr;
+  SearchOpts o{};
+  bool mixed = false;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  int n_search = 0;
+  std::vector<SearchDev> h_S;
+  std::vector<int> order;
+  std::vector<std::int64_t> n_atoms, n_mob, atom_off, act3_off;
+  std::vector<double> h_pos, h_axis;  // inputs (all atoms) for assembling outputs
+  std::vector<int> h_aatom;           // mobile atom -> local atom, per search at act_off
+  DevBuf<SearchDev> S;
+  DevBuf<int> order_d, work, err;
+  DevBuf<D4> xl, xl_init;
+  DevBuf<Packed> pk;
+  DevBuf<std::uint8_t> type;
+  DevBuf<int> aatom;
+  DevBuf<std::uint16_t> ncnt, nbr;
+  DevBuf<double> vec, vec_init, hist, out_x, out_ax;
+  DevBuf<std::int64_t> act3_d;
+  std::int64_t bytes = 0;
+  std::int64_t total_atoms = 0, total_act = 0, total_vec = 0;
+  bool tuned = false;
+  flygpu_tuning tuning{};
+  std::string tune_key;
+
+  BatchView view(int const* ord, int n_items, int budget) {
+    BatchView v{};
+    v.S = S.p;
+    v.n_search = n_search;
+    v.order = ord;
+    v.n_items = n_items;
+    v.work = work.p;
+    v.budget = budget;
+    v.o = o;
+    v.tb = eam->view();
+    v.xl = xl.p;
+    v.pk = pk.p;
+    v.type = type.p;
+    v.aatom = aatom.p;
+    v.ncnt = ncnt.p;
+    v.nbr = nbr.p;
+    v.vec = vec.p;
+    v.hist = hist.p;
+    v.err = err.p;
+    return v;
+  }
+
+  ~flygpu_batch() {
+    if (stream) cudaStreamSynchronize(stream);
+    if (own_stream && stream) cudaStreamDestroy(stream);
+  }
+};
+
+namespace flygpu {
+
+  namespace {
+
+    template <typename F>
+    int guard(F&& f) {
+      try {
+        f();
+        return FLYGPU_OK;
+      } catch (Error const& e) {
+        set_error(e.msg);
+        return e.status;
+      } catch (std::bad_alloc const&) {
+        set_error("host allocation failed");
+        return FLYGPU_OOM;
+      } catch (std::exception const& e) {
+        set_error(e.what());
+        return FLYGPU_INVALID_ARG;
+      }
+    }
+
+    template <typename T>
+    void upload(DevBuf<T>& d, std::vector<T> const& h, cudaStream_t s) {
+      d.reserve(std::max<std::size_t>(h.size(), 1));
+      if (!h.empty()) FLY_CUDA(cudaMemcpyAsync(d.p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+    }
+
+    int sm_count() {
+      int dev = 0, n = 0;
+      FLY_CUDA(cudaGetDevice(&dev));
+      FLY_CUDA(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev));
+      return n;
+    }
+
+    std::mutex g_tune_mu;
+    std::map<std::string, flygpu_tuning> g_tune_cache;
+
+    std::string cache_path() {
+      char const* p = std::getenv("FLYGPU_TUNE_CACHE");
+      return p ? std::string(p) : std::string();
+    }
+
+    void load_file_cache() {
+      std::string const p = cache_path();
+      if (p.empty()) return;
+      std::ifstream in(p);
+      std::string key;
+      flygpu_tuning t{};
+      while (in >> key >> t.lanes_per_atom >> t.threads >> t.blocks_per_sm) g_tune_cache[key] = t;
+    }
+
+    void save_file_cache() {
+      std::string const p = cache_path();
+      if (p.empty()) return;
+      std::ofstream out(p, std::ios::trunc);
+      for (auto const& [k, t] : g_tune_cache) out << k << ' ' << t.lanes_per_atom << ' ' << t.threads << ' ' << t.blocks_per_sm << '\n';
+    }
+
+  }  // namespace
+
+  void batch_build(flygpu_batch* B, flygpu_search_desc const* descs, int n_search) {
+    if (n_search <= 0) fail(FLYGPU_INVALID_ARG, "empty batch");
+    SearchOpts const& o = B->o;
+    int const nt = B->eam->n_types;
+    B->n_search = n_search;
+    B->h_S.resize(static_cast<std::size_t>(n_search));
+    std::vector<D4> h_xl;
+    std::vector<std::uint8_t> h_type;
+    std::vector<double> h_vec, h_hist;
+    std::vector<std::int64_t> h_act3;
+    std::int64_t atom_off = 0, act_off = 0, vec_off = 0, hist_off = 0;
+    for (int s = 0; s < n_search; ++s) {
+      flygpu_search_desc const& d = descs[s];
+      if (d.n <= 0 || d.n > MAX_ATOMS) fail(FLYGPU_INVALID_ARG, "atoms per search must be 1..4096");
+      if (!d.pos || !d.types || !d.frozen) fail(FLYGPU_INVALID_ARG, "search without positions, types or frozen flags");
+      bool const dimer = d.mode == FLYGPU_SEARCH_DIMER;
+      if (!dimer && d.mode != FLYGPU_SEARCH_MINIMISE) fail(FLYGPU_INVALID_ARG, "unknown search mode");
+      if (dimer && !d.axis) fail(FLYGPU_INVALID_ARG, "dimer search without an axis");
+      if (d.n_hist < 0 || (d.n_hist > 0 && !d.hist)) fail(FLYGPU_INVALID_ARG, "bad saddle history");
+      int const n = static_cast<int>(d.n);
+      SearchDev S{};
+      S.n = n;
+      S.mode = d.mode;
+      S.stage = STAGE_INIT;
+      S.status = FLYGPU_OK;
+      S.exit_code = FLYGPU_EXIT_UNINIT;
+      S.rc_list = dimer ? dimer_rc_list(o) : lbfgs_rc_list(o);
+      S.theta_tol_hist = d.theta_tol;
+      S.n_hist = dimer ? d.n_hist : 0;
+      for (int k = 0; k < 3; ++k) {
+        if (!(d.extents[k] > S.rc_list)) fail(FLYGPU_INVALID_ARG, "box extent not above the list cut-off");
+        S.L[k] = d.extents[k];
+        S.per[k] = d.periodic[k] ? 1 : 0;
+        if (S.per[k] && !(d.extents[k] > 2 * (S.rc_list + 1e-3)))
+          fail(FLYGPU_INVALID_ARG, "periodic extent must exceed twice the list cut-off in a batched search");
+        S.periodic_any |= S.per[k];
+        double const C = std::exp2(std::ceil(std::log2(d.extents[k] + 4 * S.rc_list + 1)));
+        S.shift[k] = C + 2 * S.rc_list;
+      }
+      int count_frozen = 0;
+      std::vector<int> mob;
+      for (int i = 0; i < n; ++i) {
+        if (d.types[i] >= static_cast<std::uint32_t>(nt) || d.types[i] > 255)
+          fail(FLYGPU_INVALID_ARG, "type index out of range");
+        bool const fz = d.frozen[i] != 0;
+        count_frozen += fz;
+        bool moving = !fz;
+        if (dimer && fz) moving = d.axis[3 * i] != 0 || d.axis[3 * i + 1] != 0 || d.axis[3 * i + 2] != 0;
+        if (moving) mob.push_back(i);
+      }
+      if (mob.empty()) fail(FLYGPU_INVALID_ARG, "search without mobile atoms");
+      int const na = static_cast<int>(mob.size());
+      int const M = 3 * na;
+      int const mT = dimer ? o.mT : o.mL, mR = dimer ? o.mR : 0;
+      S.na = na;
+      S.count_frozen = count_frozen;
+      S.atom_off = atom_off;
+      S.act_off = act_off;
+      S.vec_off = vec_off;
+      S.hist_off = hist_off;
+      B->h_S[static_cast<std::size_t>(s)] = S;
+      B->n_atoms.push_back(n);
+      B->n_mob.push_back(na);
+      B->atom_off.push_back(atom_off);
+      B->act3_off.push_back(3 * act_off);
+      h_act3.push_back(3 * act_off);
+      for (int i = 0; i < n; ++i) {
+        h_xl.push_back(D4{d.pos[3 * i], d.pos[3 * i + 1], d.pos[3 * i + 2], 0.0});
+        h_type.push_back(static_cast<std::uint8_t>(d.types[i]));
+      }
+      B->h_pos.insert(B->h_pos.end(), d.pos, d.pos + 3 * n);
+      if (dimer) {
+        B->h_axis.insert(B->h_axis.end(), d.axis, d.axis + 3 * n);
+      } else {
+        B->h_axis.insert(B->h_axis.end(), static_cast<std::size_t>(3 * n), 0.0);
+      }
+      for (int a : mob) B->h_aatom.push_back(a);
+      std::size_t const base = h_vec.size();
+      h_vec.resize(base + static_cast<std::size_t>((N_VEC + 2 * mT + 2 * mR) * M), 0.0);
+      double const* in_min = d.in_min ? d.in_min : d.pos;
+      for (int k = 0; k < na; ++k)
+        for (int c = 0; c < 3; ++c) {
+          int const a = mob[static_cast<std::size_t>(k)];
+          h_vec[base + static_cast<std::size_t>(V_X * M + 3 * k + c)] = d.pos[3 * a + c];
+          if (dimer) h_vec[base + static_cast<std::size_t>(V_AX * M + 3 * k + c)] = d.axis[3 * a + c];
+          h_vec[base + static_cast<std::size_t>(V_INMIN * M + 3 * k + c)] = in_min[3 * a + c];
+        }
+      for (int h = 0; h < S.n_hist; ++h)
+        for (int k = 0; k < na; ++k)
+          for (int c = 0; c < 3; ++c)
+            h_hist.push_back(d.hist[static_cast<std::size_t>(h) * 3 * n + 3 * static_cast<std::size_t>(mob[static_cast<std::size_t>(k)]) + c]);
+      atom_off += n;
+      act_off += na;
+      vec_off += static_cast<std::int64_t>(N_VEC + 2 * mT + 2 * mR) * M;
+      hist_off += static_cast<std::int64_t>(S.n_hist) * M;
+    }
+    B->total_atoms = atom_off;
+    B->total_act = act_off;
+    B->total_vec = vec_off;
+    B->order.resize(static_cast<std::size_t>(n_search));
+    std::iota(B->order.begin(), B->order.end(), 0);
+    std::stable_sort(B->order.begin(), B->order.end(),
+                     [&](int a, int b) { return B->n_atoms[static_cast<std::size_t>(a)] > B->n_atoms[static_cast<std::size_t>(b)]; });
+    cudaStream_t const st = B->stream;
+    upload(B->S, B->h_S, st);
+    upload(B->order_d, B->order, st);
+    upload(B->xl, h_xl, st);
+    upload(B->xl_init, h_xl, st);
+    upload(B->type, h_type, st);
+    upload(B->aatom, B->h_aatom, st);
+    upload(B->vec, h_vec, st);
+    upload(B->vec_init, h_vec, st);
+    upload(B->hist, h_hist, st);
+    upload(B->act3_d, h_act3, st);
+    B->pk.reserve(static_cast<std::size_t>(atom_off));
+    B->ncnt.reserve(static_cast<std::size_t>(atom_off));
+    B->nbr.reserve(static_cast<std::size_t>(atom_off) * NB_CAP);
+    B->out_x.reserve(static_cast<std::size_t>(3 * act_off));
+    B->out_ax.reserve(static_cast<std::size_t>(3 * act_off));
+    B->work.reserve(1);
+    B->err.reserve(1);
+    FLY_CUDA(cudaMemsetAsync(B->err.p, 0, sizeof(int), st));
+    FLY_CUDA(cudaStreamSynchronize(st));
+    B->bytes = static_cast<std::int64_t>(
+        B->S.n * sizeof(SearchDev) + 2 * B->xl.n * sizeof(D4) + B->pk.n * sizeof(Packed) + B->type.n + B->aatom.n * 4 +
+        B->ncnt.n * 2 + B->nbr.n * 2 + 2 * B->vec.n * 8 + B->hist.n * 8 + 2 * B->out_x.n * 8);
+    // autotune cache key: device, precision and the size bucket of the batch
+    double mean_n = static_cast<double>(atom_off) / n_search, mean_a = static_cast<double>(act_off) / n_search;
+    cudaDeviceProp prop{};
+    int dev = 0;
+    FLY_CUDA(cudaGetDevice(&dev));
+    FLY_CUDA(cudaGetDeviceProperties(&prop, dev));
+    std::ostringstream key;
+    std::string name = prop.name;
+    std::replace(name.begin(), name.end(), ' ', '_');
+    key << name << "/" << (B->mixed ? "mixed" : "fp64") << "/n" << (1 << static_cast<int>(std::lround(std::log2(std::max(1.0, mean_n)))))
+        << "/a" << (1 << static_cast<int>(std::lround(std::log2(std::max(1.0, mean_a)))));
+    B->tune_key = key.str();
+  }
+
+  void batch_reset(flygpu_batch* B) {
+    cudaStream_t const st = B->stream;
+    FLY_CUDA(cudaMemcpyAsync(B->S.p, B->h_S.data(), B->h_S.size() * sizeof(SearchDev), cudaMemcpyHostToDevice, st));
+    FLY_CUDA(cudaMemcpyAsync(B->xl.p, B->xl_init.p, static_cast<std::size_t>(B->total_atoms) * sizeof(D4),
+                             cudaMemcpyDeviceToDevice, st));
+    FLY_CUDA(cudaMemcpyAsync(B->vec.p, B->vec_init.p, static_cast<std::size_t>(B->total_vec) * sizeof(double),
+                             cudaMemcpyDeviceToDevice, st));
+    FLY_CUDA(cudaMemsetAsync(B->err.p, 0, sizeof(int), st));
+  }
+
+  void batch_launch(flygpu_batch* B, flygpu_tuning const& t, int const* ord, int n_items, int budget) {
+    if (t.threads % 32 || t.threads < 32 || t.threads > 1024) fail(FLYGPU_INVALID_ARG, "bad threads per CTA");
+    int const blocks = std::max(1, std::min(n_items, std::max(1, t.blocks_per_sm) * sm_count()));
+    FLY_CUDA(cudaMemsetAsync(B->work.p, 0, sizeof(int), B->stream));
+    search_launch(B->view(ord, n_items, budget), t.lanes_per_atom, t.threads, blocks, B->mixed, B->stream);
+  }
+
+  flygpu_tuning autotune(flygpu_batch* B) {
+    {
+      std::lock_guard<std::mutex> lk(g_tune_mu);
+      if (g_tune_cache.empty()) load_file_cache();
+      auto it = g_tune_cache.find(B->tune_key);
+      if (it != g_tune_cache.end()) return it->second;
+    }
+    // Sample: every k-th search of the size-sorted order, about two resident waves of the GPU.
+    int const sms = sm_count();
+    int const want = std::min(B->n_search, 4 * sms);
+    std::vector<int> sample;
+    for (int i = 0; i < want; ++i) sample.push_back(B->order[static_cast<std::size_t>(static_cast<std::int64_t>(i) * B->n_search / want)]);
+    DevBuf<int> ord;
+    upload(ord, sample, B->stream);
+    cudaEvent_t e0, e1;
+    FLY_CUDA(cudaEventCreate(&e0));
+    FLY_CUDA(cudaEventCreate(&e1));
+    flygpu_tuning best{4, 256, 2, 0};
+    float best_ms = 1e30f;
+    for (int lpa : {1, 2, 4, 8}) {
+      for (int threads : {128, 256}) {
+        flygpu_tuning t{lpa, threads, 0, 0};
+        int bps = 0;
+        // resident CTAs per SM for this shape
+        search_occupancy(lpa, threads, B->mixed, &bps);
+        t.blocks_per_sm = std::max(1, bps);
+        batch_reset(B);
+        FLY_CUDA(cudaEventRecord(e0, B->stream));
+        batch_launch(B, t, ord.p, want, 0);
+        FLY_CUDA(cudaEventRecord(e1, B->stream));
+        FLY_CUDA(cudaEventSynchronize(e1));
+        float ms = 0;
+        FLY_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        if (ms < best_ms) {
+          best_ms = ms;
+          best = t;
+        }
+      }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    batch_reset(B);
+    FLY_CUDA(cudaStreamSynchronize(B->stream));
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune_cache[B->tune_key] = best;
+    save_file_cache();
+    return best;
+  }
+
+}  // namespace flygpu
+
+extern "C" {
+
+void flygpu_dimer_options_default(flygpu_dimer_options* o) {
+  if (!o) return;
+  *o = flygpu_dimer_options{};
+  o->n = 10;              // dimer.hpp:58
+  o->max_steps = 1000;    // dimer.hpp:60
+  o->hist_check_freq = 5; // dimer.hpp:62
+  o->f2norm = 1e-5;       // dimer.hpp:64
+  o->skin_frac = 1.1;     // dimer.hpp:73
+  o->proj_tol = 0;
+  o->max_trust = 0.5;
+  o->min_trust = 0.05;
+  o->grow_trust = 1.5;
+  o->shrink_trust = 0.5;
+  o->convex_max = 3;
+  o->use_history = 1;
+  o->rot_n = 6;           // rotor.hpp:49
+  o->iter_max_rot = 20;   // rotor.hpp:51
+  o->delta_r = 0.001;     // rotor.hpp:53
+  o->theta_tol = 1 * M_PI / 360.;  // rotor.hpp:55
+  o->relax_in_convex = 1;
+}
+
+void flygpu_lbfgs_options_default(flygpu_lbfgs_options* o) {
+  if (!o) return;
+  *o = flygpu_lbfgs_options{};
+  o->n = 10;            // lbfgs.hpp:57
+  o->iter_max = 2000;   // lbfgs.hpp:59
+  o->f2norm = 1e-6;     // lbfgs.hpp:61
+  o->skin_frac = 1.1;   // lbfgs.hpp:70
+  o->proj_tol = 0;
+  o->max_trust = 0.5;
+  o->min_trust = 0.01;
+  o->grow_trust = 1.5;
+  o->shrink_trust = 0.5;
+}
+
+int flygpu_batch_create(flygpu_eam* eam, const flygpu_dimer_options* dimer, const flygpu_lbfgs_options* lbfgs,
+                        int precision, const flygpu_search_desc* descs, int n_search, void* stream,
+                        flygpu_batch** out) {
+  return guard([&] {
+    if (!eam || !descs || !out) fail(FLYGPU_INVALID_ARG, "null argument");
+    *out = nullptr;
+    if (precision != FLYGPU_FP64 && precision != FLYGPU_MIXED) fail(FLYGPU_INVALID_ARG, "unknown precision");
+    flygpu_dimer_options d;
+    flygpu_lbfgs_options l;
+    flygpu_dimer_options_default(&d);
+    flygpu_lbfgs_options_default(&l);
+    if (dimer) d = *dimer;
+    if (lbfgs) l = *lbfgs;
+    auto B = std::make_unique<flygpu_batch>();
+    B->eam = eam;
+    B->mixed = precision == FLYGPU_MIXED;
+    B->o = make_opts(d, l, eam->r_cut);
+    if (stream) {
+      B->stream = static_cast<cudaStream_t>(stream);
+    } else {
+      FLY_CUDA(cudaStreamCreateWithFlags(&B->stream, cudaStreamNonBlocking));
+      B->own_stream = true;
+    }
+    batch_build(B.get(), descs, n_search);
+    *out = B.release();
+  });
+}
+
+void flygpu_batch_destroy(flygpu_batch* batch) { delete batch; }
+
+int flygpu_batch_run(flygpu_batch* B, const flygpu_tuning* tuning) {
+  return guard([&] {
+    if (!B) fail(FLYGPU_INVALID_ARG, "null batch");
+    flygpu_tuning t;
+    if (tuning) {
+      t = *tuning;
+    } else {
+      if (!B->tuned) {
+        B->tuning = autotune(B);
+        B->tuned = true;
+      }
+      t = B->tuning;
+    }
+    batch_launch(B, t, B->order_d.p, B->n_search, 0);
+  });
+}
+
+int flygpu_batch_autotune(flygpu_batch* B, flygpu_tuning* best) {
+  return guard([&] {
+    if (!B || !best) fail(FLYGPU_INVALID_ARG, "null argument");
+    B->tuning = autotune(B);
+    B->tuned = true;
+    *best = B->tuning;
+  });
+}
+
+int flygpu_batch_reset(flygpu_batch* B) {
+  return guard([&] {
+    if (!B) fail(FLYGPU_INVALID_ARG, "null batch");
+    batch_reset(B);
+  });
+}
+
+int64_t flygpu_batch_device_bytes(const flygpu_batch* B) { return B ? B->bytes : 0; }
+
+int flygpu_batch_results(flygpu_batch* B, flygpu_search_result* results, double* pos_out, double* axis_out) {
+  return guard([&] {
+    if (!B) fail(FLYGPU_INVALID_ARG, "null batch");
+    cudaStream_t const st = B->stream;
+    std::vector<SearchDev> S(static_cast<std::size_t>(B->n_search));
+    FLY_CUDA(cudaMemcpyAsync(S.data(), B->S.p, S.size() * sizeof(SearchDev), cudaMemcpyDeviceToHost, st));
+    std::vector<double> ox, oa;
+    if (pos_out || axis_out) {
+      search_gather(B->view(B->order_d.p, B->n_search, 0), B->act3_d.p, B->out_x.p, B->out_ax.p, st);
+      ox.resize(static_cast<std::size_t>(3 * B->total_act));
+      oa.resize(ox.size());
+      FLY_CUDA(cudaMemcpyAsync(ox.data(), B->out_x.p, ox.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+      FLY_CUDA(cudaMemcpyAsync(oa.data(), B->out_ax.p, oa.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+    }
+    FLY_CUDA(cudaStreamSynchronize(st));
+    int first_bad = FLYGPU_OK;
+    std::int64_t pos_base = 0;
+    for (int s = 0; s < B->n_search; ++s) {
+      SearchDev const& d = S[static_cast<std::size_t>(s)];
+      if (results) {
+        flygpu_search_result& r = results[s];
+        r.exit_code = d.exit_code;
+        r.status = d.status;
+        r.steps = d.it;
+        r.pad_ = 0;
+        r.grad_calls = d.grad_calls;
+        r.curvature = d.curv;
+        r.energy = d.energy;
+      }
+      if (d.status != FLYGPU_OK && first_bad == FLYGPU_OK) first_bad = d.status;
+      std::int64_t const n = B->n_atoms[static_cast<std::size_t>(s)];
+      if (pos_out || axis_out) {
+        std::int64_t const a3 = B->act3_off[static_cast<std::size_t>(s)];
+        std::int64_t const na = B->n_mob[static_cast<std::size_t>(s)];
+        std::int64_t const a0 = a3 / 3;
+        if (pos_out) std::copy_n(&B->h_pos[static_cast<std::size_t>(3 * pos_base)], 3 * n, pos_out + 3 * pos_base);
+        if (axis_out) std::copy_n(&B->h_axis[static_cast<std::size_t>(3 * pos_base)], 3 * n, axis_out + 3 * pos_base);
+        for (std::int64_t k = 0; k < na; ++k) {
+          int const a = B->h_aatom[static_cast<std::size_t>(a0 + k)];
+          for (int c = 0; c < 3; ++c) {
+            if (pos_out) pos_out[3 * (pos_base + a) + c] = ox[static_cast<std::size_t>(a3 + 3 * k + c)];
+            if (axis_out && d.mode == MODE_DIMER) axis_out[3 * (pos_base + a) + c] = oa[static_cast<std::size_t>(a3 + 3 * k + c)];
+          }
+        }
+      }
+      pos_base += n;
+    }
+    (void)first_bad;
+  });
+}
+
+}  // extern "C"

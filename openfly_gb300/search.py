@@ -1,0 +1,227 @@
+"""Saddle searches and minimisations through libflygpu.
+
+  DimerOptions / LBFGSOptions   Dimer::Options + Rotor::Options (saddle/dimer.hpp:56-98,
+                                saddle/rotor.hpp:47-60), LBFGS::Options (minimise/LBFGS/lbfgs.hpp:56-80)
+  Batch                         many searches in one persistent launch (Master::find_batch's fan-out,
+                                saddle/find.cpp:684-732)
+  search_plain                  one search the drop-in way: host search loop, GPU List + EAM
+  Server                        continuous batching of searches (openfly_gb300.serve)
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import EAM, FP64, MIXED, check, lib
+
+DIMER, MINIMISE = 0, 1
+EXIT_SUCCESS, EXIT_CONVEX, EXIT_ITER_MAX, EXIT_COLLISION, EXIT_UNINIT = 0, -1, -2, -3, -4
+
+
+class DimerOptions(C.Structure):
+    _fields_ = [
+        ("n", C.c_int), ("max_steps", C.c_int), ("hist_check_freq", C.c_int), ("use_history", C.c_int),
+        ("f2norm", C.c_double), ("skin_frac", C.c_double), ("proj_tol", C.c_double), ("max_trust", C.c_double),
+        ("min_trust", C.c_double), ("grow_trust", C.c_double), ("shrink_trust", C.c_double),
+        ("convex_max", C.c_double),
+        ("rot_n", C.c_int), ("iter_max_rot", C.c_int), ("relax_in_convex", C.c_int), ("pad_", C.c_int),
+        ("delta_r", C.c_double), ("theta_tol", C.c_double),
+    ]
+
+    @classmethod
+    def defaults(cls, **kw) -> "DimerOptions":
+        o = cls()
+        _setup()
+        lib().flygpu_dimer_options_default(C.byref(o))
+        for k, v in kw.items():
+            setattr(o, k, v)
+        return o
+
+
+class LBFGSOptions(C.Structure):
+    _fields_ = [
+        ("n", C.c_int), ("iter_max", C.c_int), ("f2norm", C.c_double), ("skin_frac", C.c_double),
+        ("proj_tol", C.c_double), ("max_trust", C.c_double), ("min_trust", C.c_double),
+        ("grow_trust", C.c_double), ("shrink_trust", C.c_double),
+    ]
+
+    @classmethod
+    def defaults(cls, **kw) -> "LBFGSOptions":
+        o = cls()
+        _setup()
+        lib().flygpu_lbfgs_options_default(C.byref(o))
+        for k, v in kw.items():
+            setattr(o, k, v)
+        return o
+
+
+class SearchDesc(C.Structure):
+    _fields_ = [
+        ("n", C.c_int64), ("pos", C.c_void_p), ("axis", C.c_void_p), ("types", C.c_void_p),
+        ("frozen", C.c_void_p), ("extents", C.c_double * 3), ("periodic", C.c_int * 3), ("mode", C.c_int),
+        ("n_hist", C.c_int), ("hist", C.c_void_p), ("in_min", C.c_void_p), ("theta_tol", C.c_double),
+    ]
+
+
+class SearchResult(C.Structure):
+    _fields_ = [
+        ("exit_code", C.c_int), ("status", C.c_int), ("steps", C.c_int), ("pad_", C.c_int),
+        ("grad_calls", C.c_int64), ("curvature", C.c_double), ("energy", C.c_double),
+    ]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "pad_"}
+
+
+class Tuning(C.Structure):
+    _fields_ = [("lanes_per_atom", C.c_int), ("threads", C.c_int), ("blocks_per_sm", C.c_int), ("pad_", C.c_int)]
+
+    def as_dict(self) -> dict:
+        return {"lanes_per_atom": self.lanes_per_atom, "threads": self.threads, "blocks_per_sm": self.blocks_per_sm}
+
+
+_ready = False
+
+
+def _setup() -> None:
+    global _ready
+    if _ready:
+        return
+    L = lib()
+    V = C.c_void_p
+    L.flygpu_dimer_options_default.argtypes = [V]
+    L.flygpu_lbfgs_options_default.argtypes = [V]
+    L.flygpu_batch_create.argtypes = [V, V, V, C.c_int, V, C.c_int, V, C.POINTER(V)]
+    L.flygpu_batch_destroy.argtypes = [V]
+    L.flygpu_batch_run.argtypes = [V, V]
+    L.flygpu_batch_autotune.argtypes = [V, V]
+    L.flygpu_batch_reset.argtypes = [V]
+    L.flygpu_batch_results.argtypes = [V, V, V, V]
+    L.flygpu_batch_device_bytes.restype = C.c_int64
+    L.flygpu_batch_device_bytes.argtypes = [V]
+    L.flygpu_search_plain.argtypes = [V, V, V, C.c_int, V, V, V, V]
+    _ready = True
+
+
+@dataclass
+class Search:
+    """One search request: the arguments of Dimer::find_sp (or LBFGS::minimise) for one system."""
+
+    pos: np.ndarray
+    types: np.ndarray
+    frozen: np.ndarray
+    extents: np.ndarray
+    periodic: np.ndarray
+    axis: np.ndarray | None = None
+    mode: int = DIMER
+    hist: list | None = None
+    in_min: np.ndarray | None = None
+    theta_tol: float = 0.0
+
+    def desc(self, keep: list) -> SearchDesc:
+        """A SearchDesc pointing into arrays kept alive by ``keep``."""
+        def arr(a, dt):
+            a = np.ascontiguousarray(a, dtype=dt).reshape(-1)
+            keep.append(a)
+            return a.ctypes.data
+
+        d = SearchDesc()
+        d.n = int(np.asarray(self.pos).reshape(-1, 3).shape[0])
+        d.pos = arr(self.pos, np.float64)
+        d.axis = arr(self.axis, np.float64) if self.axis is not None else None
+        d.types = arr(self.types, np.uint32)
+        d.frozen = arr(self.frozen, np.uint8)
+        for k in range(3):
+            d.extents[k] = float(self.extents[k])
+            d.periodic[k] = int(self.periodic[k])
+        d.mode = self.mode
+        if self.hist:
+            h = np.ascontiguousarray(np.stack([np.asarray(x, np.float64).reshape(-1) for x in self.hist]))
+            keep.append(h)
+            d.n_hist, d.hist = h.shape[0], h.ctypes.data
+        d.in_min = arr(self.in_min, np.float64) if self.in_min is not None else None
+        d.theta_tol = self.theta_tol
+        return d
+
+    @property
+    def n(self) -> int:
+        return int(np.asarray(self.pos).reshape(-1, 3).shape[0])
+
+
+def from_cluster(cl, mode: int = DIMER) -> Search:
+    s = cl.sys
+    return Search(s.pos, s.types, s.frozen, s.extents, s.periodic, axis=cl.axis if mode == DIMER else None,
+                  mode=mode)
+
+
+class Batch:
+    """Many searches resident on the GPU, run by one persistent launch."""
+
+    def __init__(self, eam: EAM, searches: list[Search], precision: int = MIXED,
+                 dimer: DimerOptions | None = None, lbfgs: LBFGSOptions | None = None, stream: int | None = None):
+        _setup()
+        self.searches = searches
+        keep: list = []
+        descs = (SearchDesc * len(searches))(*[s.desc(keep) for s in searches])
+        h = C.c_void_p()
+        self.dimer = dimer or DimerOptions.defaults()
+        self.lbfgs = lbfgs or LBFGSOptions.defaults()
+        check(lib().flygpu_batch_create(eam.h, C.byref(self.dimer), C.byref(self.lbfgs), precision, descs,
+                                        len(searches), stream, C.byref(h)), "Batch")
+        self.h = h
+        self.eam = eam
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().flygpu_batch_destroy(self.h)
+            self.h = None
+
+    def run(self, tuning: Tuning | None = None) -> None:
+        check(lib().flygpu_batch_run(self.h, C.byref(tuning) if tuning is not None else None), "Batch.run")
+
+    def autotune(self) -> Tuning:
+        t = Tuning()
+        check(lib().flygpu_batch_autotune(self.h, C.byref(t)), "Batch.autotune")
+        return t
+
+    def reset(self) -> None:
+        check(lib().flygpu_batch_reset(self.h), "Batch.reset")
+
+    @property
+    def device_bytes(self) -> int:
+        return lib().flygpu_batch_device_bytes(self.h)
+
+    def results(self, positions: bool = True):
+        """(list of result dicts, list of (n,3) positions, list of (n,3) axes); waits for the batch."""
+        n = len(self.searches)
+        res = (SearchResult * n)()
+        tot = sum(s.n for s in self.searches)
+        pos = np.zeros(3 * tot) if positions else None
+        ax = np.zeros(3 * tot) if positions else None
+        check(lib().flygpu_batch_results(self.h, res, pos.ctypes.data if positions else None,
+                                         ax.ctypes.data if positions else None), "Batch.results")
+        out_p, out_a, o = [], [], 0
+        if positions:
+            for s in self.searches:
+                out_p.append(pos[3 * o:3 * (o + s.n)].reshape(-1, 3))
+                out_a.append(ax[3 * o:3 * (o + s.n)].reshape(-1, 3))
+                o += s.n
+        return [r.as_dict() for r in res], out_p, out_a
+
+
+def search_plain(eam: EAM, s: Search, precision: int = FP64, dimer: DimerOptions | None = None,
+                 lbfgs: LBFGSOptions | None = None):
+    """One search the drop-in way; returns (result dict, positions (n,3), axis (n,3))."""
+    _setup()
+    keep: list = []
+    d = s.desc(keep)
+    pos = np.zeros(3 * s.n)
+    ax = np.zeros(3 * s.n)
+    r = SearchResult()
+    dimer = dimer or DimerOptions.defaults()
+    lbfgs = lbfgs or LBFGSOptions.defaults()
+    check(lib().flygpu_search_plain(eam.h, C.byref(dimer), C.byref(lbfgs), precision, C.byref(d), pos.ctypes.data,
+                                    ax.ctypes.data, C.byref(r)), "search_plain")
+    return r.as_dict(), pos.reshape(-1, 3), ax.reshape(-1, 3)

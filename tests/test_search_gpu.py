@@ -1,0 +1,145 @@
+"""Batched and plain GPU searches vs the oracle's Dimer::find_sp / LBFGS::minimise.
+
+Tolerances: saddle (and minimum) energies within 1 meV of the binary64 oracle for every search that
+both converge (the barrier-height bar); exit codes equal for at least 90 % of the searches (a dimer
+search can branch to a different saddle on rounding-level differences in its reductions).
+"""
+import numpy as np
+import pytest
+
+from openfly_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+E_TOL = 1e-3  # eV
+
+
+@pytest.fixture(scope="module")
+def search_mod(gpu):
+    from openfly_gb300 import search
+
+    return search
+
+
+@pytest.fixture(scope="module")
+def clusters():
+    return W.config3(n=16, seed=11)
+
+
+def c3_options(S, O):
+    gpu_opt = S.DimerOptions.defaults(n=6, rot_n=6, f2norm=1e-3, max_steps=1000)
+    orc_opt = O.DimerOptions.defaults(n=6, rot_n=6, f2norm=1e-3, max_steps=1000)
+    return gpu_opt, orc_opt
+
+
+def oracle_energy(O, odata, s, pos):
+    nl = O.List(s.extents, s.periodic, odata.r_cut)
+    nl.rebuild(pos, 1)
+    return O.eam_energy(odata, nl, s.types)
+
+
+def run_oracle(O, odata, opt, cl):
+    s = cl.sys
+    r = O.dimer_find_sp(odata, opt, s.extents, s.periodic, s.pos, cl.axis, s.types, s.frozen)
+    r["energy"] = oracle_energy(O, odata, s, r["x"])
+    return r
+
+
+def compare(results, refs, label):
+    both = [(a, b) for a, b in zip(results, refs) if a["exit_code"] == 0 and b["exit"] == 0]
+    same_exit = sum(a["exit_code"] == b["exit"] for a, b in zip(results, refs))
+    assert same_exit >= 0.9 * len(refs), (label, [(a["exit_code"], b["exit"]) for a, b in zip(results, refs)])
+    errs = [abs(a["energy"] - b["energy"]) for a, b in both]
+    assert both, label
+    assert max(errs) < E_TOL, (label, errs)
+    return errs
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_batched_dimer_matches_oracle(gpu, oracle, odata, geam, search_mod, clusters, precision):
+    S, O = search_mod, oracle
+    gopt, oopt = c3_options(S, O)
+    prec = gpu.FP64 if precision == "fp64" else gpu.MIXED
+    b = S.Batch(geam, [S.from_cluster(c) for c in clusters], precision=prec, dimer=gopt)
+    b.run(S.Tuning(4, 128, 2))
+    res, pos, ax = b.results()
+    assert all(r["status"] == 0 for r in res), res
+    refs = [run_oracle(O, odata, oopt, c) for c in clusters]
+    compare(res, refs, precision)
+    # the reported energy is the energy of the returned positions
+    for r, p, c in zip(res, pos, clusters):
+        assert abs(r["energy"] - oracle_energy(O, odata, c.sys, p)) < 1e-4
+
+
+def test_same_alone_and_in_mix(gpu, geam, search_mod, clusters):
+    S = search_mod
+    gopt = S.DimerOptions.defaults(n=6, rot_n=6, f2norm=1e-3)
+    t = S.Tuning(4, 128, 2)
+    mix = S.Batch(geam, [S.from_cluster(c) for c in clusters], precision=gpu.MIXED, dimer=gopt)
+    mix.run(t)
+    res_mix, pos_mix, _ = mix.results()
+    for k in (0, 5, len(clusters) - 1):
+        alone = S.Batch(geam, [S.from_cluster(clusters[k])], precision=gpu.MIXED, dimer=gopt)
+        alone.run(t)
+        r, p, _ = alone.results()
+        assert r[0]["exit_code"] == res_mix[k]["exit_code"]
+        assert r[0]["energy"] == res_mix[k]["energy"]
+        assert np.array_equal(p[0], pos_mix[k])
+
+
+def test_batch_rerun_after_reset_is_identical(gpu, geam, search_mod, clusters):
+    S = search_mod
+    b = S.Batch(geam, [S.from_cluster(c) for c in clusters[:6]], precision=gpu.MIXED,
+                dimer=S.DimerOptions.defaults(n=6, f2norm=1e-3))
+    b.run(S.Tuning(2, 128, 2))
+    r1, p1, _ = b.results()
+    b.reset()
+    b.run(S.Tuning(2, 128, 2))
+    r2, p2, _ = b.results()
+    assert r1 == r2
+    assert all(np.array_equal(a, c) for a, c in zip(p1, p2))
+
+
+def test_plain_path_matches_oracle(gpu, oracle, odata, geam, search_mod, clusters):
+    S, O = search_mod, oracle
+    gopt, oopt = c3_options(S, O)
+    res, refs = [], []
+    for c in clusters[:4]:
+        r, p, _ = S.search_plain(geam, S.from_cluster(c), gpu.FP64, dimer=gopt)
+        res.append(r)
+        refs.append(run_oracle(O, odata, oopt, c))
+    compare(res, refs, "plain")
+
+
+def test_config1_periodic_search(gpu, oracle, odata, geam, search_mod):
+    # 431-atom periodic cell, vacancy neighbour perturbed as Master::perturb does, f2norm 1e-3.
+    S, O = search_mod, oracle
+    s = W.config1()
+    pos, axis = W.perturb(s, s.meta["centre"], np.random.default_rng(4))
+    gopt, oopt = c3_options(S, O)
+    ref = O.dimer_find_sp(odata, oopt, s.extents, s.periodic, pos, axis, s.types, s.frozen)
+    ref["energy"] = oracle_energy(O, odata, s, ref["x"])
+    srch = S.Search(pos, s.types, s.frozen, s.extents, s.periodic, axis=axis)
+    plain, _, _ = S.search_plain(geam, srch, gpu.FP64, dimer=gopt)
+    b = S.Batch(geam, [srch], precision=gpu.FP64, dimer=gopt)
+    b.run(S.Tuning(4, 256, 1))
+    batched = b.results()[0][0]
+    for r in (plain, batched):
+        assert r["exit_code"] == ref["exit"]
+        if ref["exit"] == 0:
+            assert abs(r["energy"] - ref["energy"]) < E_TOL
+
+
+def test_minimise_matches_oracle(gpu, oracle, odata, geam, search_mod, clusters):
+    S, O = search_mod, oracle
+    lopt = S.LBFGSOptions.defaults(f2norm=1e-4)
+    olopt = O.LBFGSOptions.defaults(f2norm=1e-4)
+    subset = clusters[:6]
+    b = S.Batch(geam, [S.from_cluster(c, mode=S.MINIMISE) for c in subset], precision=gpu.FP64, lbfgs=lopt)
+    b.run(S.Tuning(4, 128, 2))
+    res, pos, _ = b.results()
+    for r, p, c in zip(res, pos, subset):
+        s = c.sys
+        failed, iters, x, g = O.lbfgs_minimise(odata, olopt, s.extents, s.periodic, s.pos, s.types, s.frozen)
+        assert r["exit_code"] == int(failed)
+        assert abs(r["energy"] - oracle_energy(O, odata, s, x)) < E_TOL
