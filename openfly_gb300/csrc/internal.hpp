@@ -202,6 +202,7 @@ struct flygpu_list {
   flygpu::DevBuf<int> pref;      // reference slot id of each physical slot
   flygpu::DevBuf<int> ptype;     // type of each physical slot
   flygpu::DevBuf<flygpu::Packed> packed;
+  flygpu::DevBuf<float4> hi;     // binary32 hi parts of the offset coordinates (build prefilter)
   flygpu::DevBuf<int> cell_count, cell_start, cell_fill, members;
   flygpu::DevBuf<int> real_phys;  // physical slot of the j-th real atom in cell order
   flygpu::DevBuf<int> nbr;        // [nb_cap][n] physical neighbour slots, column per atom

@@ -13,6 +13,9 @@
 // the reference. Positions are D4 (one 32-byte sector per gather); neighbour lists are stored
 // column-per-atom ([k][j]) so a warp's loads of the k-th neighbour are coalesced.
 
+#include <algorithm>
+#include <cmath>
+
 #include "internal.hpp"
 
 namespace flygpu {
@@ -208,17 +211,31 @@ namespace flygpu {
       if (flag[p]) real_phys[scan[p]] = static_cast<int>(p);
     }
 
+    // Binary32 hi parts of the offset coordinates of every physical slot (for the build prefilter).
+    __global__ void k_hi(D4 const* __restrict__ pos, std::int64_t slots, float4* __restrict__ hi, double sx, double sy,
+                         double sz) {
+      std::int64_t const p = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+      if (p >= slots) return;
+      D4 const v = pos[p];
+      hi[p] = make_float4(static_cast<float>(v.x + sx), static_cast<float>(v.y + sy), static_cast<float>(v.z + sz), 0.f);
+    }
+
     // Per real atom j (cell order): own cell (skipping itself) then the adjacent cells in increasing
     // index, each walked from its last physical slot down. Records physical neighbour slots.
-    __global__ void k_build(D4 const* __restrict__ pos, int const* __restrict__ real_phys,
+    // The binary32 hi coordinates lie in one binade per axis, so their differences are exact and the
+    // binary32 r^2 is within `band` of the binary64 one; only candidates inside that band take the
+    // binary64 test (dx*dx + dy*dy) + dz*dz < rc^2, which is the decision the reference makes.
+    __global__ void k_build(D4 const* __restrict__ pos, float4 const* __restrict__ hi, int const* __restrict__ real_phys,
                             int const* __restrict__ cell_ref, int const* __restrict__ pref,
                             int const* __restrict__ start, int const* __restrict__ count, std::int64_t n, GridDesc g,
-                            int cap, int* __restrict__ nbr, int* __restrict__ ncount, int* __restrict__ maxc) {
+                            float band, int cap, int* __restrict__ nbr, int* __restrict__ ncount,
+                            int* __restrict__ maxc) {
       std::int64_t const j = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
       if (j >= n) return;
       int const p = real_phys[j];
-      D4 const ri = pos[p];
+      float4 const hp = hi[p];
       double const rc2 = g.rc * g.rc;
+      float const lo_f = static_cast<float>(rc2) - band, hi_f = static_cast<float>(rc2) + band;
       int const c = cell_ref[pref[p]];
       int const s0 = g.shape[0], s1 = g.shape[1], s2 = g.shape[2];
       int const cx = c % s0, cy = (c / s0) % s1, cz = c / (s0 * s1);
@@ -227,9 +244,16 @@ namespace flygpu {
         int const b = start[cell];
         for (int q = b + count[cell] - 1; q >= b; --q) {
           if (same && q == p) continue;
-          D4 const rq = pos[q];
-          double const dx = ri.x - rq.x, dy = ri.y - rq.y, dz = ri.z - rq.z;
-          if ((dx * dx + dy * dy) + dz * dz < rc2) {
+          float4 const hq = hi[q];
+          float const fx = hp.x - hq.x, fy = hp.y - hq.y, fz = hp.z - hq.z;
+          float const r2f = fx * fx + fy * fy + fz * fz;
+          bool in = r2f < lo_f;
+          if (!in && r2f <= hi_f) {
+            D4 const ri = pos[p], rq = pos[q];
+            double const dx = ri.x - rq.x, dy = ri.y - rq.y, dz = ri.z - rq.z;
+            in = (dx * dx + dy * dy) + dz * dz < rc2;
+          }
+          if (in) {
             if (k < cap) nbr[static_cast<std::int64_t>(k) * n + j] = q;
             ++k;
           }
@@ -451,15 +475,25 @@ namespace flygpu {
     exclusive_scan(L->flag_p.p, L->scan_p.p, slots, L->scan_tmp.p, L->scan_tmp.n, s);
     launch(k_real_compact, blocks_for(slots), T, 0, s, L->flag_p.p, L->scan_p.p, slots, L->real_phys.p);
     FLY_CUDA(cudaGetLastError());
-    // Neighbour lists; grow the capacity once if any atom overflowed it.
+    // Neighbour lists; grow the capacity once if any atom overflowed it. The first capacity is the
+    // expected count at the real-atom density plus headroom.
     L->ncount.reserve(static_cast<std::size_t>(n));
-    if (L->nb_cap == 0) L->nb_cap = 64;
+    L->hi.reserve(static_cast<std::size_t>(slots));
+    launch(k_hi, blocks_for(slots), T, 0, s, L->pos.p, slots, L->hi.p, L->shift[0], L->shift[1], L->shift[2]);
+    if (L->nb_cap == 0) {
+      double const vol = g.L[0] * g.L[1] * g.L[2];
+      double const expect = 4.18879 * g.rc * g.rc * g.rc * static_cast<double>(n) / vol;
+      L->nb_cap = std::min(1024, (static_cast<int>(1.25 * expect) + 16 + 7) / 8 * 8);
+    }
+    // Error bound of the binary32 r^2 (hi parts carry at most half an ulp of the offset binade each).
+    double ulp = 0;
+    for (int k = 0; k < 3; ++k) ulp = std::max(ulp, std::ldexp(1.0, std::ilogb(L->shift[k] + g.L[k]) - 23));
+    float const band = static_cast<float>(4.0 * g.rc * std::sqrt(3.0) * ulp + 1e-5 * g.rc * g.rc + 1e-6);
     for (int attempt = 0; attempt < 2; ++attempt) {
       L->nbr.reserve(static_cast<std::size_t>(L->nb_cap) * static_cast<std::size_t>(n));
       FLY_CUDA(cudaMemsetAsync(L->counters.p + 2, 0, sizeof(int), s));
-      launch(k_build, blocks_for(n, 128), 128, 0, s, L->pos.p, L->real_phys.p, L->cell_ref.p, L->pref.p, L->cell_start.p,
-                                                 L->cell_count.p, n, g, L->nb_cap, L->nbr.p, L->ncount.p,
-                                                 L->counters.p + 2);
+      launch(k_build, blocks_for(n, 128), 128, 0, s, L->pos.p, L->hi.p, L->real_phys.p, L->cell_ref.p, L->pref.p,
+             L->cell_start.p, L->cell_count.p, n, g, band, L->nb_cap, L->nbr.p, L->ncount.p, L->counters.p + 2);
       FLY_CUDA(cudaGetLastError());
       sync_small(L, 3);
       int const need = L->h_small.p[2];

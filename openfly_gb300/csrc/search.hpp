@@ -9,7 +9,7 @@ namespace flygpu {
 
   constexpr int NB_CAP = 96;       // neighbour capacity per atom inside a search (uint16 local indices)
   constexpr int MAX_ATOMS = 4096;  // atoms per search (local indices fit in uint16 with room to spare)
-  constexpr int MAX_HIST = 8;      // L-BFGS history length supported on the device
+  constexpr int MAX_HIST = 16;     // L-BFGS history length supported on the device
   constexpr int N_VEC = 15;        // fixed per-DOF vectors of a search (see Vec below)
 
   enum Mode : int { MODE_DIMER = 0, MODE_MINIMISE = 1 };

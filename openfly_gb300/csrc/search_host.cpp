@@ -52,7 +52,7 @@ namespace flygpu {
     o.shrink_trust_l = l.shrink_trust;
     o.r_cut = r_cut;
     if (o.mT < 1 || o.mT > MAX_HIST || o.mR < 1 || o.mR > MAX_HIST || o.mL < 1 || o.mL > MAX_HIST)
-      fail(FLYGPU_INVALID_ARG, "L-BFGS history lengths must be 1..8 on the device");
+      fail(FLYGPU_INVALID_ARG, "L-BFGS history lengths must be 1..16 on the device");
     if (o.max_steps < 0 || o.iter_max_l < 0 || o.hist_check_freq < 1) fail(FLYGPU_INVALID_ARG, "bad iteration limits");
     return o;
   }
