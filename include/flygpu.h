@@ -195,6 +195,38 @@ int flygpu_search_plain(flygpu_eam* eam, const flygpu_dimer_options* dimer, cons
                         int precision, const flygpu_search_desc* desc, double* pos_out, double* axis_out,
                         flygpu_search_result* result);
 
+/* ---------------------------------------------------------------- served searches
+ * Continuous batching of search requests. The reference's Master::find_mechs runs each environment's
+ * searches batch by batch (saddle/find.cpp:374-372 find_n, 684-755 find_batch); this server takes
+ * searches as they are emitted, keeps every search's positions, axis and L-BFGS history resident on the
+ * device, admits them while the sum of their device footprints stays under hbm_budget_bytes, and
+ * advances all admitted searches together steps_per_tick translation steps at a time. Finished slots
+ * are refilled at the next tick. The server handle is internally synchronised. */
+typedef struct flygpu_server flygpu_server;
+
+typedef struct {
+  uint64_t id;
+  flygpu_search_result result;
+  double latency_ms;  /* submit to completion */
+  double queue_ms;    /* submit to admission */
+} flygpu_served;
+
+typedef struct {
+  int64_t pending, active, completed, ticks, hbm_used, hbm_budget;
+} flygpu_server_stats;
+
+int flygpu_server_create(flygpu_eam* eam, const flygpu_dimer_options* dimer, const flygpu_lbfgs_options* lbfgs,
+                         int precision, int64_t hbm_budget_bytes, int max_active, int steps_per_tick,
+                         const flygpu_tuning* tuning, flygpu_server** out);
+void flygpu_server_destroy(flygpu_server* srv);
+/* Queues one search (inputs are copied); id receives its request id. */
+int flygpu_server_submit(flygpu_server* srv, const flygpu_search_desc* desc, uint64_t* id);
+/* Returns up to max finished searches, waiting up to wait_ms for the first. */
+int flygpu_server_poll(flygpu_server* srv, int max, int wait_ms, flygpu_served* out, int* n_out);
+/* Copies a polled search's final positions / axis (3n each, may be NULL) and forgets it. */
+int flygpu_server_take(flygpu_server* srv, uint64_t id, double* pos_out, double* axis_out);
+int flygpu_server_get_stats(flygpu_server* srv, flygpu_server_stats* stats);
+
 #ifdef __cplusplus
 }
 #endif

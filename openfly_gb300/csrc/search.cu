@@ -607,14 +607,14 @@ namespace flygpu {
       bool const dimer = S->mode == MODE_DIMER;
       c.mT = dimer ? o.mT : o.mL;
       c.mR = dimer ? o.mR : 0;
-      c.xl = bv.xl + S->atom_off;
-      c.pk = bv.pk + S->atom_off;
-      c.ty = bv.type + S->atom_off;
-      c.aatom = bv.aatom + S->act_off;
-      c.ncnt = bv.ncnt + S->atom_off;
-      c.nbr = bv.nbr + S->atom_off * NB_CAP;
-      c.v = bv.vec + S->vec_off;
-      c.hist = bv.hist + S->hist_off;
+      c.xl = S->xl;
+      c.pk = S->pk;
+      c.ty = S->type;
+      c.aatom = S->aatom;
+      c.ncnt = S->ncnt;
+      c.nbr = S->nbr;
+      c.v = S->vec;
+      c.hist = S->hist;
       c.rc2 = o.r_cut * o.r_cut;
       c.rc2f = static_cast<float>(c.rc2);
       c.periodic = S->periodic_any != 0;
@@ -783,12 +783,13 @@ namespace flygpu {
     template <bool MIXED, int LPA>
     __global__ void k_search(BatchView bv) {
       __shared__ Blk sh;
+      int const n_items = bv.n_items_dev ? *bv.n_items_dev : bv.n_items;
       for (;;) {
         if (threadIdx.x == 0) sh.item = atomicAdd(bv.work, 1);
         __syncthreads();
         int const item = sh.item;
         __syncthreads();
-        if (item >= bv.n_items) break;
+        if (item >= n_items) break;
         run<MIXED, LPA>(bv, sh, bv.order[item]);
       }
     }
@@ -811,7 +812,7 @@ namespace flygpu {
       if (s >= bv.n_search) return;
       SearchDev const& S = bv.S[s];
       int const M = 3 * S.na;
-      double const* v = bv.vec + S.vec_off;
+      double const* v = S.vec;
       std::int64_t const o = act3[s];
       for (int e = threadIdx.x; e < M; e += blockDim.x) {
         ox[o + e] = v[static_cast<std::int64_t>(V_X) * M + e];
@@ -831,6 +832,41 @@ namespace flygpu {
     }
 
   }  // namespace
+
+  SearchLayout search_layout(int n, int na, int n_vec_doubles, int n_hist_doubles) {
+    auto up = [](std::size_t b) { return (b + 255) / 256 * 256; };
+    SearchLayout l{};
+    std::size_t o = 0;
+    l.xl = o;
+    o += up(sizeof(D4) * static_cast<std::size_t>(n));
+    l.pk = o;
+    o += up(sizeof(Packed) * static_cast<std::size_t>(n));
+    l.vec = o;
+    o += up(sizeof(double) * static_cast<std::size_t>(n_vec_doubles));
+    l.hist = o;
+    o += up(sizeof(double) * static_cast<std::size_t>(n_hist_doubles));
+    l.aatom = o;
+    o += up(sizeof(int) * static_cast<std::size_t>(na));
+    l.nbr = o;
+    o += up(sizeof(std::uint16_t) * static_cast<std::size_t>(n) * NB_CAP);
+    l.ncnt = o;
+    o += up(sizeof(std::uint16_t) * static_cast<std::size_t>(n));
+    l.type = o;
+    o += up(static_cast<std::size_t>(n));
+    l.total = o;
+    return l;
+  }
+
+  void search_bind(SearchDev& S, char* base, SearchLayout const& l) {
+    S.xl = reinterpret_cast<D4*>(base + l.xl);
+    S.pk = reinterpret_cast<Packed*>(base + l.pk);
+    S.type = reinterpret_cast<std::uint8_t*>(base + l.type);
+    S.aatom = reinterpret_cast<int*>(base + l.aatom);
+    S.ncnt = reinterpret_cast<std::uint16_t*>(base + l.ncnt);
+    S.nbr = reinterpret_cast<std::uint16_t*>(base + l.nbr);
+    S.vec = reinterpret_cast<double*>(base + l.vec);
+    S.hist = reinterpret_cast<double const*>(base + l.hist);
+  }
 
   void search_gather(BatchView const& v, std::int64_t const* d_act3_off, double* out_x, double* out_ax,
                      cudaStream_t s) {

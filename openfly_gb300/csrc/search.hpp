@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cstdint>
+#include <vector>
 
 #include "internal.hpp"
 
@@ -55,7 +56,15 @@ namespace flygpu {
     double shift[3];        // binary32 packed-coordinate offset per axis
     double rc_list;         // neighbour-list cut-off of this search
     double theta_tol_hist;  // collision angle (Master::find_batch, find.cpp:692)
-    std::int64_t atom_off, act_off, vec_off, hist_off;
+    // this search's arrays (inside a batch's shared buffers or a served request's own block)
+    D4* xl;                 // list positions per atom (w = F')
+    Packed* pk;             // binary32 records per atom
+    std::uint8_t* type;     // per atom
+    int* aatom;             // per mobile atom: local atom index
+    std::uint16_t* ncnt;    // per atom
+    std::uint16_t* nbr;     // [NB_CAP][n]
+    double* vec;            // (N_VEC + 2 mT + 2 mR) vectors of 3 na doubles
+    double const* hist;     // n_hist vectors of 3 na doubles (previous saddle points)
     double trust, acc, convex, curv, energy;
     std::int64_t grad_calls;
     double rhoT[MAX_HIST], alphaT[MAX_HIST];
@@ -66,24 +75,27 @@ namespace flygpu {
     int n_search;
     int const* order;         // work items -> search index
     int n_items;
+    int const* n_items_dev;   // if set, the item count is read from device memory (graph replays)
     int* work;                // atomic work counter
     int budget;               // translation steps per launch (<= 0: run to completion)
     SearchOpts o;
     TablesView tb;
-    D4* xl;                   // list positions per atom (w = F')
-    Packed* pk;               // binary32 records per atom
-    std::uint8_t* type;       // per atom
-    int* aidx;                // per atom: mobile index or -1
-    int* aatom;               // per mobile atom: local atom index
-    std::uint16_t* ncnt;      // per atom
-    std::uint16_t* nbr;       // [NB_CAP][n] per search, at atom_off * NB_CAP
-    double* vec;              // per search: (N_VEC + 2 mT + 2 mR) vectors of 3 na doubles
-    double const* hist;       // per search: n_hist vectors of 3 na doubles (previous saddle points)
-    int* err;                 // batch error word
+  };
+
+  // Byte offsets of one search's arrays inside its block (256-byte aligned parts).
+  struct SearchLayout {
+    std::size_t xl, pk, type, aatom, ncnt, nbr, vec, hist, total;
   };
 
   // search.cu
   void search_launch(BatchView const& v, int lanes_per_atom, int threads, int blocks, bool mixed, cudaStream_t s);
   void search_occupancy(int lanes_per_atom, int threads, bool mixed, int* blocks_per_sm);
+  SearchLayout search_layout(int n, int na, int n_vec_doubles, int n_hist_doubles);
+  void search_bind(SearchDev& S, char* base, SearchLayout const& l);
+
+  // search_host.cpp: fill one search's state and initial arrays (image at byte `at` of img).
+  SearchLayout search_prepare(SearchOpts const& o, int n_types, flygpu_search_desc const& d, SearchDev& S,
+                              std::vector<int>& mob, std::vector<char>& img, std::size_t at);
+  SearchOpts make_opts(flygpu_dimer_options const& d, flygpu_lbfgs_options const& l, double r_cut);
 
 }  // namespace flygpu

@@ -83,16 +83,13 @@ struct flygpu_batch {
   std::vector<double> h_pos, h_axis;  // inputs (all atoms) for assembling outputs
   std::vector<int> h_aatom;           // mobile atom -> local atom, per search at act_off
   DevBuf<SearchDev> S;
-  DevBuf<int> order_d, work, err;
-  DevBuf<D4> xl, xl_init;
-  DevBuf<Packed> pk;
-  DevBuf<std::uint8_t> type;
-  DevBuf<int> aatom;
-  DevBuf<std::uint16_t> ncnt, nbr;
-  DevBuf<double> vec, vec_init, hist, out_x, out_ax;
+  DevBuf<int> order_d, work;
+  DevBuf<char> block, block_init;  // every search's arrays (search_layout), and their initial image
+  DevBuf<double> out_x, out_ax;
   DevBuf<std::int64_t> act3_d;
   std::int64_t bytes = 0;
-  std::int64_t total_atoms = 0, total_act = 0, total_vec = 0;
+  std::int64_t total_atoms = 0, total_act = 0;
+  std::size_t block_bytes = 0;
   bool tuned = false;
   flygpu_tuning tuning{};
   std::string tune_key;
@@ -107,15 +104,6 @@ struct flygpu_batch {
     v.budget = budget;
     v.o = o;
     v.tb = eam->view();
-    v.xl = xl.p;
-    v.pk = pk.p;
-    v.type = type.p;
-    v.aatom = aatom.p;
-    v.ncnt = ncnt.p;
-    v.nbr = nbr.p;
-    v.vec = vec.p;
-    v.hist = hist.p;
-    v.err = err.p;
     return v;
   }
 
@@ -185,134 +173,137 @@ namespace flygpu {
 
   }  // namespace
 
+  // Fills S (geometry, state) for one description and writes its initial arrays into `img` at the
+  // search's block offset. Returns the search's block layout. Shared by batches and the server.
+  SearchLayout search_prepare(SearchOpts const& o, int n_types, flygpu_search_desc const& d, SearchDev& S,
+                              std::vector<int>& mob, std::vector<char>& img, std::size_t at) {
+    if (d.n <= 0 || d.n > MAX_ATOMS) fail(FLYGPU_INVALID_ARG, "atoms per search must be 1..4096");
+    if (!d.pos || !d.types || !d.frozen) fail(FLYGPU_INVALID_ARG, "search without positions, types or frozen flags");
+    bool const dimer = d.mode == FLYGPU_SEARCH_DIMER;
+    if (!dimer && d.mode != FLYGPU_SEARCH_MINIMISE) fail(FLYGPU_INVALID_ARG, "unknown search mode");
+    if (dimer && !d.axis) fail(FLYGPU_INVALID_ARG, "dimer search without an axis");
+    if (d.n_hist < 0 || (d.n_hist > 0 && !d.hist)) fail(FLYGPU_INVALID_ARG, "bad saddle history");
+    int const n = static_cast<int>(d.n);
+    S = SearchDev{};
+    S.n = n;
+    S.mode = d.mode;
+    S.stage = STAGE_INIT;
+    S.status = FLYGPU_OK;
+    S.exit_code = FLYGPU_EXIT_UNINIT;
+    S.rc_list = dimer ? dimer_rc_list(o) : lbfgs_rc_list(o);
+    S.theta_tol_hist = d.theta_tol;
+    S.n_hist = dimer ? d.n_hist : 0;
+    for (int k = 0; k < 3; ++k) {
+      if (!(d.extents[k] > S.rc_list)) fail(FLYGPU_INVALID_ARG, "box extent not above the list cut-off");
+      S.L[k] = d.extents[k];
+      S.per[k] = d.periodic[k] ? 1 : 0;
+      if (S.per[k] && !(d.extents[k] > 2 * (S.rc_list + 1e-3)))
+        fail(FLYGPU_INVALID_ARG, "periodic extent must exceed twice the list cut-off in a batched search");
+      S.periodic_any |= S.per[k];
+      double const C = std::exp2(std::ceil(std::log2(d.extents[k] + 4 * S.rc_list + 1)));
+      S.shift[k] = C + 2 * S.rc_list;
+    }
+    int count_frozen = 0;
+    mob.clear();
+    for (int i = 0; i < n; ++i) {
+      if (d.types[i] >= static_cast<std::uint32_t>(n_types) || d.types[i] > 255)
+        fail(FLYGPU_INVALID_ARG, "type index out of range");
+      bool const fz = d.frozen[i] != 0;
+      count_frozen += fz;
+      bool moving = !fz;
+      if (dimer && fz) moving = d.axis[3 * i] != 0 || d.axis[3 * i + 1] != 0 || d.axis[3 * i + 2] != 0;
+      if (moving) mob.push_back(i);
+    }
+    if (mob.empty()) fail(FLYGPU_INVALID_ARG, "search without mobile atoms");
+    int const na = static_cast<int>(mob.size());
+    int const M = 3 * na;
+    int const mT = dimer ? o.mT : o.mL, mR = dimer ? o.mR : 0;
+    S.na = na;
+    S.count_frozen = count_frozen;
+    SearchLayout const l = search_layout(n, na, (N_VEC + 2 * mT + 2 * mR) * M, S.n_hist * M);
+    if (img.size() < at + l.total) img.resize(at + l.total, 0);
+    char* base = img.data() + at;
+    D4* xl = reinterpret_cast<D4*>(base + l.xl);
+    std::uint8_t* ty = reinterpret_cast<std::uint8_t*>(base + l.type);
+    int* aat = reinterpret_cast<int*>(base + l.aatom);
+    double* v = reinterpret_cast<double*>(base + l.vec);
+    double* h = reinterpret_cast<double*>(base + l.hist);
+    for (int i = 0; i < n; ++i) {
+      xl[i] = D4{d.pos[3 * i], d.pos[3 * i + 1], d.pos[3 * i + 2], 0.0};
+      ty[i] = static_cast<std::uint8_t>(d.types[i]);
+    }
+    double const* in_min = d.in_min ? d.in_min : d.pos;
+    for (int k = 0; k < na; ++k) {
+      int const a = mob[static_cast<std::size_t>(k)];
+      aat[k] = a;
+      for (int c = 0; c < 3; ++c) {
+        v[V_X * M + 3 * k + c] = d.pos[3 * a + c];
+        if (dimer) v[V_AX * M + 3 * k + c] = d.axis[3 * a + c];
+        v[V_INMIN * M + 3 * k + c] = in_min[3 * a + c];
+        for (int hh = 0; hh < S.n_hist; ++hh)
+          h[hh * M + 3 * k + c] = d.hist[static_cast<std::size_t>(hh) * 3 * static_cast<std::size_t>(n) + 3 * static_cast<std::size_t>(a) + static_cast<std::size_t>(c)];
+      }
+    }
+    return l;
+  }
+
   void batch_build(flygpu_batch* B, flygpu_search_desc const* descs, int n_search) {
     if (n_search <= 0) fail(FLYGPU_INVALID_ARG, "empty batch");
-    SearchOpts const& o = B->o;
-    int const nt = B->eam->n_types;
     B->n_search = n_search;
     B->h_S.resize(static_cast<std::size_t>(n_search));
-    std::vector<D4> h_xl;
-    std::vector<std::uint8_t> h_type;
-    std::vector<double> h_vec, h_hist;
+    std::vector<char> img;
+    std::vector<SearchLayout> lay(static_cast<std::size_t>(n_search));
+    std::vector<std::size_t> at(static_cast<std::size_t>(n_search));
     std::vector<std::int64_t> h_act3;
-    std::int64_t atom_off = 0, act_off = 0, vec_off = 0, hist_off = 0;
+    std::vector<int> mob;
+    std::size_t off = 0;
+    std::int64_t atoms = 0, act = 0;
     for (int s = 0; s < n_search; ++s) {
       flygpu_search_desc const& d = descs[s];
-      if (d.n <= 0 || d.n > MAX_ATOMS) fail(FLYGPU_INVALID_ARG, "atoms per search must be 1..4096");
-      if (!d.pos || !d.types || !d.frozen) fail(FLYGPU_INVALID_ARG, "search without positions, types or frozen flags");
-      bool const dimer = d.mode == FLYGPU_SEARCH_DIMER;
-      if (!dimer && d.mode != FLYGPU_SEARCH_MINIMISE) fail(FLYGPU_INVALID_ARG, "unknown search mode");
-      if (dimer && !d.axis) fail(FLYGPU_INVALID_ARG, "dimer search without an axis");
-      if (d.n_hist < 0 || (d.n_hist > 0 && !d.hist)) fail(FLYGPU_INVALID_ARG, "bad saddle history");
-      int const n = static_cast<int>(d.n);
-      SearchDev S{};
-      S.n = n;
-      S.mode = d.mode;
-      S.stage = STAGE_INIT;
-      S.status = FLYGPU_OK;
-      S.exit_code = FLYGPU_EXIT_UNINIT;
-      S.rc_list = dimer ? dimer_rc_list(o) : lbfgs_rc_list(o);
-      S.theta_tol_hist = d.theta_tol;
-      S.n_hist = dimer ? d.n_hist : 0;
-      for (int k = 0; k < 3; ++k) {
-        if (!(d.extents[k] > S.rc_list)) fail(FLYGPU_INVALID_ARG, "box extent not above the list cut-off");
-        S.L[k] = d.extents[k];
-        S.per[k] = d.periodic[k] ? 1 : 0;
-        if (S.per[k] && !(d.extents[k] > 2 * (S.rc_list + 1e-3)))
-          fail(FLYGPU_INVALID_ARG, "periodic extent must exceed twice the list cut-off in a batched search");
-        S.periodic_any |= S.per[k];
-        double const C = std::exp2(std::ceil(std::log2(d.extents[k] + 4 * S.rc_list + 1)));
-        S.shift[k] = C + 2 * S.rc_list;
-      }
-      int count_frozen = 0;
-      std::vector<int> mob;
-      for (int i = 0; i < n; ++i) {
-        if (d.types[i] >= static_cast<std::uint32_t>(nt) || d.types[i] > 255)
-          fail(FLYGPU_INVALID_ARG, "type index out of range");
-        bool const fz = d.frozen[i] != 0;
-        count_frozen += fz;
-        bool moving = !fz;
-        if (dimer && fz) moving = d.axis[3 * i] != 0 || d.axis[3 * i + 1] != 0 || d.axis[3 * i + 2] != 0;
-        if (moving) mob.push_back(i);
-      }
-      if (mob.empty()) fail(FLYGPU_INVALID_ARG, "search without mobile atoms");
-      int const na = static_cast<int>(mob.size());
-      int const M = 3 * na;
-      int const mT = dimer ? o.mT : o.mL, mR = dimer ? o.mR : 0;
-      S.na = na;
-      S.count_frozen = count_frozen;
-      S.atom_off = atom_off;
-      S.act_off = act_off;
-      S.vec_off = vec_off;
-      S.hist_off = hist_off;
-      B->h_S[static_cast<std::size_t>(s)] = S;
+      SearchDev& S = B->h_S[static_cast<std::size_t>(s)];
+      at[static_cast<std::size_t>(s)] = off;
+      lay[static_cast<std::size_t>(s)] = search_prepare(B->o, B->eam->n_types, d, S, mob, img, off);
+      off += lay[static_cast<std::size_t>(s)].total;
+      int const n = S.n, na = S.na;
       B->n_atoms.push_back(n);
       B->n_mob.push_back(na);
-      B->atom_off.push_back(atom_off);
-      B->act3_off.push_back(3 * act_off);
-      h_act3.push_back(3 * act_off);
-      for (int i = 0; i < n; ++i) {
-        h_xl.push_back(D4{d.pos[3 * i], d.pos[3 * i + 1], d.pos[3 * i + 2], 0.0});
-        h_type.push_back(static_cast<std::uint8_t>(d.types[i]));
-      }
+      B->atom_off.push_back(atoms);
+      B->act3_off.push_back(3 * act);
+      h_act3.push_back(3 * act);
       B->h_pos.insert(B->h_pos.end(), d.pos, d.pos + 3 * n);
-      if (dimer) {
+      if (d.mode == FLYGPU_SEARCH_DIMER) {
         B->h_axis.insert(B->h_axis.end(), d.axis, d.axis + 3 * n);
       } else {
         B->h_axis.insert(B->h_axis.end(), static_cast<std::size_t>(3 * n), 0.0);
       }
-      for (int a : mob) B->h_aatom.push_back(a);
-      std::size_t const base = h_vec.size();
-      h_vec.resize(base + static_cast<std::size_t>((N_VEC + 2 * mT + 2 * mR) * M), 0.0);
-      double const* in_min = d.in_min ? d.in_min : d.pos;
-      for (int k = 0; k < na; ++k)
-        for (int c = 0; c < 3; ++c) {
-          int const a = mob[static_cast<std::size_t>(k)];
-          h_vec[base + static_cast<std::size_t>(V_X * M + 3 * k + c)] = d.pos[3 * a + c];
-          if (dimer) h_vec[base + static_cast<std::size_t>(V_AX * M + 3 * k + c)] = d.axis[3 * a + c];
-          h_vec[base + static_cast<std::size_t>(V_INMIN * M + 3 * k + c)] = in_min[3 * a + c];
-        }
-      for (int h = 0; h < S.n_hist; ++h)
-        for (int k = 0; k < na; ++k)
-          for (int c = 0; c < 3; ++c)
-            h_hist.push_back(d.hist[static_cast<std::size_t>(h) * 3 * n + 3 * static_cast<std::size_t>(mob[static_cast<std::size_t>(k)]) + c]);
-      atom_off += n;
-      act_off += na;
-      vec_off += static_cast<std::int64_t>(N_VEC + 2 * mT + 2 * mR) * M;
-      hist_off += static_cast<std::int64_t>(S.n_hist) * M;
+      B->h_aatom.insert(B->h_aatom.end(), mob.begin(), mob.end());
+      atoms += n;
+      act += na;
     }
-    B->total_atoms = atom_off;
-    B->total_act = act_off;
-    B->total_vec = vec_off;
+    B->total_atoms = atoms;
+    B->total_act = act;
+    B->block_bytes = off;
+    cudaStream_t const st = B->stream;
+    B->block.reserve(off);
+    B->block_init.reserve(off);
+    for (int s = 0; s < n_search; ++s)
+      search_bind(B->h_S[static_cast<std::size_t>(s)], B->block.p + at[static_cast<std::size_t>(s)], lay[static_cast<std::size_t>(s)]);
     B->order.resize(static_cast<std::size_t>(n_search));
     std::iota(B->order.begin(), B->order.end(), 0);
     std::stable_sort(B->order.begin(), B->order.end(),
                      [&](int a, int b) { return B->n_atoms[static_cast<std::size_t>(a)] > B->n_atoms[static_cast<std::size_t>(b)]; });
-    cudaStream_t const st = B->stream;
     upload(B->S, B->h_S, st);
     upload(B->order_d, B->order, st);
-    upload(B->xl, h_xl, st);
-    upload(B->xl_init, h_xl, st);
-    upload(B->type, h_type, st);
-    upload(B->aatom, B->h_aatom, st);
-    upload(B->vec, h_vec, st);
-    upload(B->vec_init, h_vec, st);
-    upload(B->hist, h_hist, st);
     upload(B->act3_d, h_act3, st);
-    B->pk.reserve(static_cast<std::size_t>(atom_off));
-    B->ncnt.reserve(static_cast<std::size_t>(atom_off));
-    B->nbr.reserve(static_cast<std::size_t>(atom_off) * NB_CAP);
-    B->out_x.reserve(static_cast<std::size_t>(3 * act_off));
-    B->out_ax.reserve(static_cast<std::size_t>(3 * act_off));
+    FLY_CUDA(cudaMemcpyAsync(B->block_init.p, img.data(), off, cudaMemcpyHostToDevice, st));
+    FLY_CUDA(cudaMemcpyAsync(B->block.p, B->block_init.p, off, cudaMemcpyDeviceToDevice, st));
+    B->out_x.reserve(static_cast<std::size_t>(3 * act));
+    B->out_ax.reserve(static_cast<std::size_t>(3 * act));
     B->work.reserve(1);
-    B->err.reserve(1);
-    FLY_CUDA(cudaMemsetAsync(B->err.p, 0, sizeof(int), st));
     FLY_CUDA(cudaStreamSynchronize(st));
-    B->bytes = static_cast<std::int64_t>(
-        B->S.n * sizeof(SearchDev) + 2 * B->xl.n * sizeof(D4) + B->pk.n * sizeof(Packed) + B->type.n + B->aatom.n * 4 +
-        B->ncnt.n * 2 + B->nbr.n * 2 + 2 * B->vec.n * 8 + B->hist.n * 8 + 2 * B->out_x.n * 8);
+    B->bytes = static_cast<std::int64_t>(B->S.n * sizeof(SearchDev) + 2 * off + 2 * B->out_x.n * 8);
     // autotune cache key: device, precision and the size bucket of the batch
-    double mean_n = static_cast<double>(atom_off) / n_search, mean_a = static_cast<double>(act_off) / n_search;
+    double mean_n = static_cast<double>(atoms) / n_search, mean_a = static_cast<double>(act) / n_search;
     cudaDeviceProp prop{};
     int dev = 0;
     FLY_CUDA(cudaGetDevice(&dev));
@@ -328,11 +319,7 @@ namespace flygpu {
   void batch_reset(flygpu_batch* B) {
     cudaStream_t const st = B->stream;
     FLY_CUDA(cudaMemcpyAsync(B->S.p, B->h_S.data(), B->h_S.size() * sizeof(SearchDev), cudaMemcpyHostToDevice, st));
-    FLY_CUDA(cudaMemcpyAsync(B->xl.p, B->xl_init.p, static_cast<std::size_t>(B->total_atoms) * sizeof(D4),
-                             cudaMemcpyDeviceToDevice, st));
-    FLY_CUDA(cudaMemcpyAsync(B->vec.p, B->vec_init.p, static_cast<std::size_t>(B->total_vec) * sizeof(double),
-                             cudaMemcpyDeviceToDevice, st));
-    FLY_CUDA(cudaMemsetAsync(B->err.p, 0, sizeof(int), st));
+    FLY_CUDA(cudaMemcpyAsync(B->block.p, B->block_init.p, B->block_bytes, cudaMemcpyDeviceToDevice, st));
   }
 
   void batch_launch(flygpu_batch* B, flygpu_tuning const& t, int const* ord, int n_items, int budget) {
