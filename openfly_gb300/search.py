@@ -211,6 +211,81 @@ class Batch:
         return [r.as_dict() for r in res], out_p, out_a
 
 
+class Served(C.Structure):
+    _fields_ = [("id", C.c_uint64), ("result", SearchResult), ("latency_ms", C.c_double), ("queue_ms", C.c_double)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("pending", C.c_int64), ("active", C.c_int64), ("completed", C.c_int64), ("ticks", C.c_int64),
+                ("hbm_used", C.c_int64), ("hbm_budget", C.c_int64)]
+
+
+class Server:
+    """Continuous batching of searches (flygpu_server): submit as requests arrive, poll completions."""
+
+    def __init__(self, eam: EAM, precision: int = MIXED, hbm_budget_bytes: int = 40 << 30, max_active: int = 1024,
+                 steps_per_tick: int = 8, tuning: Tuning | None = None, dimer: DimerOptions | None = None,
+                 lbfgs: LBFGSOptions | None = None):
+        _setup()
+        L = lib()
+        V = C.c_void_p
+        L.flygpu_server_create.argtypes = [V, V, V, C.c_int, C.c_int64, C.c_int, C.c_int, V, C.POINTER(V)]
+        L.flygpu_server_destroy.argtypes = [V]
+        L.flygpu_server_submit.argtypes = [V, V, C.POINTER(C.c_uint64)]
+        L.flygpu_server_poll.argtypes = [V, C.c_int, C.c_int, V, C.POINTER(C.c_int)]
+        L.flygpu_server_take.argtypes = [V, C.c_uint64, V, V]
+        L.flygpu_server_get_stats.argtypes = [V, V]
+        self.dimer = dimer or DimerOptions.defaults()
+        self.lbfgs = lbfgs or LBFGSOptions.defaults()
+        self.tuning = tuning
+        h = C.c_void_p()
+        check(L.flygpu_server_create(eam.h, C.byref(self.dimer), C.byref(self.lbfgs), precision, hbm_budget_bytes,
+                                     max_active, steps_per_tick, C.byref(tuning) if tuning is not None else None,
+                                     C.byref(h)), "Server")
+        self.h = h
+        self.eam = eam
+        self.n_atoms: dict[int, int] = {}
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            lib().flygpu_server_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+    def submit(self, s: Search) -> int:
+        keep: list = []
+        d = s.desc(keep)
+        rid = C.c_uint64()
+        check(lib().flygpu_server_submit(self.h, C.byref(d), C.byref(rid)), "Server.submit")
+        self.n_atoms[rid.value] = s.n
+        return rid.value
+
+    def poll(self, max_n: int = 256, wait_ms: int = 0) -> list[dict]:
+        buf = (Served * max_n)()
+        n = C.c_int()
+        check(lib().flygpu_server_poll(self.h, max_n, wait_ms, buf, C.byref(n)), "Server.poll")
+        out = []
+        for k in range(n.value):
+            r = buf[k]
+            d = r.result.as_dict()
+            d.update(id=r.id, latency_ms=r.latency_ms, queue_ms=r.queue_ms)
+            out.append(d)
+        return out
+
+    def take(self, rid: int):
+        """(positions (n,3), axis (n,3)) of a polled request; forgets it."""
+        n = self.n_atoms.pop(rid)
+        pos, ax = np.zeros(3 * n), np.zeros(3 * n)
+        check(lib().flygpu_server_take(self.h, rid, pos.ctypes.data, ax.ctypes.data), "Server.take")
+        return pos.reshape(-1, 3), ax.reshape(-1, 3)
+
+    def stats(self) -> dict:
+        st = ServerStats()
+        check(lib().flygpu_server_get_stats(self.h, C.byref(st)), "Server.stats")
+        return {k: getattr(st, k) for k, _ in st._fields_}
+
+
 def search_plain(eam: EAM, s: Search, precision: int = FP64, dimer: DimerOptions | None = None,
                  lbfgs: LBFGSOptions | None = None):
     """One search the drop-in way; returns (result dict, positions (n,3), axis (n,3))."""

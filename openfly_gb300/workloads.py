@@ -188,6 +188,92 @@ def cluster(rng: np.random.Generator, radius: float, shell: float = 5.5, n_vac: 
     return Cluster(s, axis, centre)
 
 
+def config4_box(seed: int = 16, cells: int = 20, n_vac: int = 5, n_h: int = 20) -> System:
+    """The served workload's system: cells^3 bcc Fe (20^3 = 16,000 sites) with n_vac vacancies and n_h H
+    on random distinct tetrahedral sites, seeded sigma = 0.02 A noise, periodic."""
+    rng = np.random.default_rng(seed)
+    sites = bcc_sites(cells, cells, cells, A_FE)
+    keep = np.ones(sites.shape[0], dtype=bool)
+    vac = rng.choice(sites.shape[0], n_vac, replace=False)
+    keep[vac] = False
+    pick = rng.choice(cells ** 3 * TETRA.shape[0], n_h, replace=False)
+    cz, rem = np.divmod(pick // TETRA.shape[0], cells * cells)
+    cy, cx = np.divmod(rem, cells)
+    h = (np.stack([cx, cy, cz], axis=1) + TETRA[pick % TETRA.shape[0]]) * A_FE
+    pos = np.concatenate([sites[keep], h])
+    pos += rng.normal(0.0, 0.02, pos.shape)
+    types = np.concatenate([np.zeros(int(keep.sum()), np.uint32), np.ones(n_h, np.uint32)])
+    n = pos.shape[0]
+    return System(pos, types, np.zeros(n, np.uint8), np.full(3, cells * A_FE), np.ones(3, np.int32),
+                  dict(vacancies=sites[vac], n_fe=int(keep.sum())))
+
+
+def environment_centres(box: System, n_env: int, rng: np.random.Generator) -> np.ndarray:
+    """Atoms whose local environments a KMC step would emit searches for: the H atoms, the nearest
+    neighbours of each vacancy, then random Fe atoms."""
+    L = box.extents
+    cand = list(np.nonzero(box.types == H)[0])
+    for v in box.meta["vacancies"]:
+        d = box.pos - v
+        d -= L * np.round(d / L)
+        cand += list(np.argsort(np.linalg.norm(d, axis=1))[:8])
+    cand = list(dict.fromkeys(int(c) for c in cand))
+    rng.shuffle(cand)
+    while len(cand) < n_env:
+        cand.append(int(rng.integers(0, box.meta["n_fe"])))
+    return np.array(cand[:n_env])
+
+
+def cut_request(box: System, centre: int, radius: float, rng: np.random.Generator, shell: float = 5.5,
+                margin: float = 3.0, stddev: float = 0.6, r_pert: float = 4.0) -> Cluster:
+    """One served search request: the atoms within ``radius`` of ``centre`` (minimum image) as a
+    non-periodic cluster with a frozen outer shell, perturbed and given an axis as Master::perturb does
+    (find.cpp:1147-1214: sigma ~ N(stddev, stddev/3) > 0, envelope 1 - r/r_pert on the mobile
+    neighbours within r_pert, full noise on the centre)."""
+    L = box.extents
+    d = box.pos - box.pos[centre]
+    d -= L * np.round(d / L)
+    r = np.linalg.norm(d, axis=1)
+    sel = np.nonzero(r <= radius)[0]
+    sel = sel[np.argsort(r[sel], kind="stable")]
+    pos = d[sel].copy()
+    rr = r[sel]
+    frozen = (rr > radius - shell).astype(np.uint8)
+    frozen[0] = 0
+    sub = System(pos, box.types[sel].copy(), frozen, np.ones(3), np.zeros(3, np.int32))
+    s = -1.0
+    while s < 0:
+        s = rng.normal(stddev, stddev / 3.0)
+    axis = np.zeros_like(pos)
+    near = (rr < r_pert) & (frozen == 0)
+    near[0] = False
+    k = int(near.sum())
+    pos[near] += rng.normal(0.0, s, (k, 3)) * (1.0 - rr[near] / r_pert)[:, None]
+    axis[near] = rng.normal(0.0, 1.0, (k, 3))
+    pos[0] += rng.normal(0.0, s, 3)
+    axis[0] = rng.normal(0.0, 1.0, 3)
+    axis /= np.linalg.norm(axis)
+    lo = pos.min(axis=0) - margin
+    pos -= lo
+    sub.pos = pos
+    sub.extents = pos.max(axis=0) + margin
+    sub.meta = dict(radius=radius, box_index=sel)
+    return Cluster(sub, axis, 0)
+
+
+def config4_requests(n_env: int = 96, seed: int = 44, r_min: float = 6.0, r_max: float = 11.0,
+                     per_env: tuple[int, int] = (8, 32)):
+    """The served request stream: n_env new local environments in the 16,000-site box, each emitting
+    8-32 searches of clusters with radius ~ U(r_min, r_max). Returns a list of (environment, Cluster)."""
+    rng = np.random.default_rng(seed)
+    box = config4_box()
+    out = []
+    for e, c in enumerate(environment_centres(box, n_env, rng)):
+        for _ in range(int(rng.integers(per_env[0], per_env[1] + 1))):
+            out.append((e, cut_request(box, int(c), rng.uniform(r_min, r_max), rng)))
+    return out
+
+
 def config3(n: int = 4096, seed: int = 7, r_min: float = 6.0, r_max: float = 11.0) -> list[Cluster]:
     """n independent clusters with radii ~ U(r_min, r_max), 0-3 vacancies, 0-2 H (all seeded)."""
     rng = np.random.default_rng(seed)
