@@ -116,10 +116,15 @@ def measured_peak_hbm() -> tuple[float, str]:
     return 6800.0, "fallback"
 
 
-def traffic_from_profile(kernel: str) -> float | None:
+def traffic_from_profile(kernel: str, atoms: int) -> float | None:
+    """DRAM bytes (read + write) of one launch of `kernel` at `atoms` atoms, from the committed ncu
+    capture of a smaller case (profiles/eam_passes_config2.md), scaled by atom count: the traffic of a
+    pass grows in proportion to the atoms it processes."""
     p = os.path.join(ROOT, "profiles", "c2_dram_traffic.json")
     if os.path.exists(p):
-        return json.load(open(p)).get(kernel)
+        k = json.load(open(p)).get(kernel)
+        if k:
+            return k["bytes_per_atom"] * atoms
     return None
 
 
@@ -301,7 +306,7 @@ def ours(args):
     dom_ms, dom_cnt = ktimes[dom]
     per_atom = ALGO_BYTES_FORCE if dom == "force" else ALGO_BYTES_DENSITY
     achieved = per_atom * n / (dom_ms / dom_cnt * 1e-3) / 1e9
-    traffic = traffic_from_profile("k_force32" if dom == "force" else "k_density32")
+    traffic = traffic_from_profile("k_force32" if dom == "force" else "k_density32", n)
 
     line = {
         "metric": METRIC, "value": value, "unit": "atom-evals/s", "n_gpus": world, "steps": args.steps,
