@@ -77,7 +77,8 @@ def test_tick_length_and_budget_do_not_change_results(gpu, geam, S, requests):
 
 
 def test_request_over_budget_is_rejected(gpu, geam, S, requests):
-    srv = S.Server(geam, hbm_budget_bytes=1 << 16, max_active=4)
+    # a 1 KiB budget is below any request's device footprint (its neighbour columns alone are larger)
+    srv = S.Server(geam, hbm_budget_bytes=1 << 10, max_active=4)
     with pytest.raises(gpu.FlyGPUError) as e:
         srv.submit(S.from_cluster(requests[0]))
     assert e.value.status == gpu.OOM
