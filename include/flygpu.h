@@ -114,6 +114,22 @@ int flygpu_eam_energy_gradient_device(flygpu_eam* eam, flygpu_list* list, const 
                                       const uint8_t* d_frozen, int precision, double* d_energy,
                                       double* d_grad);
 
+/* For callers that cannot allocate device memory (a host framework that owns every device allocation,
+ * a real-time loop that must not touch the allocator after start-up, a caller holding only borrowed
+ * device pointers). No reference counterpart. Computes the same energy and gradient as
+ * flygpu_eam_energy_gradient with FLYGPU_FP64 for one system of at most FLYGPU_NOALLOC_MAX_ATOMS atoms,
+ * from device inputs into device outputs, and allocates nothing: its scratch is a fixed array inside
+ * the library (about 33 KB per GPU, held until the process exits) and pairs are found by a minimum-image
+ * scan without a neighbour list (periodic extents must exceed twice the cut-off). The first call on
+ * each device looks up that array's device address, so make the first call before any stream capture.
+ * Calls share the array, so calls that overlap on the GPU race; the call waits for its stream before
+ * returning so it can report spline and type errors. Larger systems are rejected with
+ * FLYGPU_INVALID_ARG. d_pos: 3n doubles; d_grad: 3n doubles; d_energy: 1 double. */
+#define FLYGPU_NOALLOC_MAX_ATOMS 4096
+int flygpu_eam_energy_gradient_noalloc(const flygpu_eam* eam, const double* d_pos, const uint32_t* d_types,
+                                       const uint8_t* d_frozen, int64_t n, const double extents[3],
+                                       const int periodic[3], double* d_energy, double* d_grad, void* stream);
+
 /* ---------------------------------------------------------------- searches */
 
 /* Dimer::Options (saddle/dimer.hpp:56-98) then Rotor::Options (saddle/rotor.hpp:47-60). */
