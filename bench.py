@@ -190,6 +190,107 @@ def config_dict(s, args):
             "parallelism": f"replicas x{args.gpus}"}
 
 
+# ----------------------------------------------------------------------------- search metrics
+
+def search_metrics(fly, args) -> dict:
+    """Configs 3 and 4: batched searches/s (one persistent launch over 4096 clusters), the plain
+    one-search-at-a-time drop-in GPU path on a sample, binary32-pair vs binary64 saddle energies, and
+    the served path's searches/s with p50/p99 latency under Poisson arrivals."""
+    import threading
+
+    import torch
+
+    from openfly_gb300 import search as S
+    from openfly_gb300 import workloads as W
+
+    eam = fly.EAM(W.TABLE)
+    opt = S.DimerOptions.defaults(n=6, rot_n=6, f2norm=1e-3, max_steps=1000)
+    clusters = W.config3(n=args.searches, seed=7)
+    reqs = [S.from_cluster(c) for c in clusters]
+    out = {"config3": {"searches": len(reqs), "mean_atoms": float(np.mean([r.n for r in reqs])),
+                       "options": "m=6 (translation and rotation), |F| < 1e-3 eV/A, <= 1000 steps"}}
+    l0 = fly.launch_count()
+    runs = {}
+    for prec, name in ((fly.MIXED, "mixed"), (fly.FP64, "fp64")):
+        b = S.Batch(eam, reqs, precision=prec, dimer=opt)
+        tune = b.autotune()
+        best = None
+        for _ in range(2):
+            b.reset()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            t0 = time.perf_counter()
+            b.run(tune)
+            res, _, _ = b.results(positions=False)
+            dt = time.perf_counter() - t0
+            best = dt if best is None else min(best, dt)
+        runs[name] = res
+        ex = [r["exit_code"] for r in res]
+        out["config3"][name] = {"searches_per_s": len(reqs) / best, "seconds": best, "tuning": tune.as_dict(),
+                                "converged": ex.count(0), "convex": ex.count(-1), "iter_max": ex.count(-2),
+                                "errors": sum(r["status"] != 0 for r in res),
+                                "grad_calls_mean": float(np.mean([r["grad_calls"] for r in res]))}
+    both = [(a["energy"], b_["energy"]) for a, b_ in zip(runs["mixed"], runs["fp64"])
+            if a["exit_code"] == 0 and b_["exit_code"] == 0]
+    err = np.abs(np.array([a - b_ for a, b_ in both])) * 1e3 if both else np.zeros(0)
+    out["config3"]["saddle_energy_err_mixed_vs_fp64_meV"] = {
+        "n": int(err.size), "max": float(err.max()) if err.size else None,
+        "p99": float(np.percentile(err, 99)) if err.size else None,
+        "same_exit_fraction": float(np.mean([a["exit_code"] == b_["exit_code"]
+                                             for a, b_ in zip(runs["mixed"], runs["fp64"])]))}
+    # plain drop-in path, one search at a time, on an evenly spread sample
+    sample = reqs[:: max(1, len(reqs) // args.plain_sample)][: args.plain_sample]
+    lat = []
+    t0 = time.perf_counter()
+    for r in sample:
+        t1 = time.perf_counter()
+        S.search_plain(eam, r, fly.MIXED, dimer=opt)
+        lat.append(1e3 * (time.perf_counter() - t1))
+    plain = len(sample) / (time.perf_counter() - t0)
+    out["config3"]["plain_one_at_a_time"] = {"searches_per_s": plain, "sample": len(sample),
+                                             "p50_ms": float(np.percentile(lat, 50)),
+                                             "p99_ms": float(np.percentile(lat, 99))}
+    out["config3"]["batched_over_plain"] = out["config3"]["mixed"]["searches_per_s"] / plain
+    # served stream (config 4)
+    stream = [S.from_cluster(c) for _, c in W.config4_requests()]
+    srv = S.Server(eam, precision=fly.MIXED, hbm_budget_bytes=40 << 30, max_active=2048,
+                   steps_per_tick=args.steps_per_tick, tuning=out["config3"]["mixed"] and S.Tuning(
+                       **out["config3"]["mixed"]["tuning"]), dimer=opt)
+    rng = np.random.default_rng(1)
+    arrivals = np.cumsum(rng.exponential(1.0 / args.arrival_rate, len(stream)))
+    done: list = []
+    stop = threading.Event()
+
+    def poller():
+        while len(done) < len(stream) and not (stop.is_set() and len(done) >= len(stream)):
+            done.extend(srv.poll(512, wait_ms=20))
+            if stop.is_set() and srv.stats()["pending"] == 0 and srv.stats()["active"] == 0 and len(done) >= len(stream):
+                break
+
+    th = threading.Thread(target=poller)
+    th.start()
+    t0 = time.perf_counter()
+    for k, r in enumerate(stream):
+        while time.perf_counter() - t0 < arrivals[k]:
+            pass
+        srv.submit(r)
+    stop.set()
+    th.join(timeout=600)
+    elapsed = time.perf_counter() - t0
+    st = srv.stats()
+    srv.close()
+    lat = np.array([d["latency_ms"] for d in done])
+    ex = [d["exit_code"] for d in done]
+    out["config4"] = {"requests": len(stream), "completed": len(done), "arrival_rate_per_s": args.arrival_rate,
+                      "searches_per_s": len(done) / elapsed, "p50_ms": float(np.percentile(lat, 50)),
+                      "p99_ms": float(np.percentile(lat, 99)), "steps_per_tick": args.steps_per_tick,
+                      "ticks": st["ticks"], "converged": ex.count(0), "hbm_budget_bytes": 40 << 30,
+                      "plain_service_p50_ms": out["config3"]["plain_one_at_a_time"]["p50_ms"],
+                      "plain_service_p99_ms": out["config3"]["plain_one_at_a_time"]["p99_ms"]}
+    out["gpu_launches"] = int(fly.launch_count() - l0)
+    return out
+
+
 # ----------------------------------------------------------------------------- GPU leg
 
 def ours(args):
@@ -323,6 +424,8 @@ def ours(args):
         "gpu_launches": int(launches),
         "clocks": clk,
     }
+    if rank == 0 and not args.no_searches:
+        line["searches"] = search_metrics(fly, args)
     if rank == 0 and not args.no_cpu and world == 1:
         threads = os.cpu_count() or 1
         os.environ.setdefault("OMP_NUM_THREADS", str(threads))
@@ -345,6 +448,11 @@ def main():
     ap.add_argument("--cells", type=int, default=80, help="bcc cells per side (80 -> 1,024,000 sites)")
     ap.add_argument("--cpu-steps", type=int, default=3, help="steps of the bounded CPU baseline sample")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-searches", action="store_true", help="skip the search metrics (configs 3 and 4)")
+    ap.add_argument("--searches", type=int, default=4096, help="clusters in the batched search run")
+    ap.add_argument("--plain-sample", type=int, default=32, help="searches timed on the plain path")
+    ap.add_argument("--arrival-rate", type=float, default=1500.0, help="served requests per second (Poisson)")
+    ap.add_argument("--steps-per-tick", type=int, default=8, help="translation steps per serving tick")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")

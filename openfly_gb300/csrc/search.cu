@@ -1,14 +1,18 @@
 // search.cu -- batched, resumable dimer searches and L-BFGS minimisations, one CTA per search.
 //
 // Device restatement of the reference's search stack for many independent searches at once:
-//   Dimer::find_sp        src/saddle/dimer.cpp:28-171
-//   Rotor::eff_gradient   src/saddle/rotor.cpp:49-164 (trans_proj rotor.cpp:33-47)
+//   Dimer::find_sp         src/saddle/dimer.cpp:28-171
+//   Rotor::eff_gradient    src/saddle/rotor.cpp:49-164 (trans_proj rotor.cpp:33-47)
 //   StepLBFGS::newton_step src/minimise/LBFGS/lbfgs_core.cpp:29-87
-//   LBFGS::minimise       src/minimise/LBFGS/lbfgs.cpp:29-115
-//   EAM::gradient/energy  src/potential/EAM/eam.cpp:33-120 over a per-search neighbour list
-// A persistent grid pulls searches from an atomic work counter (largest first). The CTA owning a
-// search runs its control flow uniformly: every thread holds the same scalars, vectors are split
-// over threads by degree of freedom, and each dot product is one binary64 block reduction.
+//   LBFGS::minimise        src/minimise/LBFGS/lbfgs.cpp:29-115
+//   EAM::gradient/energy   src/potential/EAM/eam.cpp:33-120 over a per-search neighbour list
+// A persistent grid pulls searches from an atomic work counter (largest first). Inside the CTA that
+// owns a search, the neighbour build and the EAM passes use every thread; the search's vector
+// algebra and control (two-loop recursions, dots, rotor angles, trust radius) run in warp 0 alone,
+// with warp-level binary64 reductions and no block barriers, and warp 0 passes its decisions to the
+// other warps through shared memory. GB300 issues binary64 at ~1/70 of binary32, so keeping the
+// scalar and vector binary64 work to one warp (and transcendental scalars to one lane) is what keeps
+// the search off the binary64 pipe.
 // Vectors are compacted to mobile atoms (not frozen, or with a non-zero axis component): the
 // reference's vectors are exactly zero elsewhere, so the compacted algebra is the same algebra.
 // State lives in global memory (L2-resident while the search runs) and is saved at translation-step
@@ -21,52 +25,46 @@ namespace flygpu {
 
   namespace {
 
-    constexpr int MAXW = 32;
-
-    struct Blk {
-      double red[4 * MAXW];
-      double bc[4];
-      double rhoR[MAX_HIST], alphaR[MAX_HIST];
-      int item;
-      int flag;
-    };
+    constexpr unsigned FULL = 0xffffffffu;
 
     enum : int { F_OOB = 1, F_NLIST = 2 };
+    enum : int { ACT_GO = 0, ACT_REBUILD = 1, ACT_STOP = 2 };
+
+    struct Blk {
+      double red[32];
+      double rhoR[MAX_HIST], alphaR[MAX_HIST];
+      double curv;
+      int n_need;  // atoms in the current needed list
+      int item;
+      int flag;    // error bits (F_OOB, F_NLIST), any thread
+      int action;  // warp 0 -> block
+    };
 
     __device__ inline double warp_sum(double v) {
-      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
       return v;
     }
 
-    // Sums K values over the block; every thread receives the totals.
-    template <int K>
-    __device__ inline void bsum(double (&v)[K], Blk& sh) {
+    // Block-wide sum (all threads receive it); only used for the final energy.
+    __device__ inline double block_sum(double v, Blk& sh) {
       int const lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-#pragma unroll
-      for (int k = 0; k < K; ++k) v[k] = warp_sum(v[k]);
-      if (lane == 0) {
-#pragma unroll
-        for (int k = 0; k < K; ++k) sh.red[w * K + k] = v[k];
-      }
+      v = warp_sum(v);
       __syncthreads();
-      if (w == 0) {
-#pragma unroll
-        for (int k = 0; k < K; ++k) {
-          double x = lane < nw ? sh.red[lane * K + k] : 0.0;
-          x = warp_sum(x);
-          if (lane == 0) sh.bc[k] = x;
-        }
-      }
+      if (lane == 0) sh.red[w] = v;
       __syncthreads();
-#pragma unroll
-      for (int k = 0; k < K; ++k) v[k] = sh.bc[k];
+      double s = 0;
+      for (int k = 0; k < nw; ++k) s += sh.red[k];
+      __syncthreads();
+      return s;
     }
 
-    __device__ inline double dot1(double const* a, double const* b, int M, Blk& sh) {
-      double v[1] = {0.0};
-      for (int e = threadIdx.x; e < M; e += blockDim.x) v[0] += a[e] * b[e];
-      bsum<1>(v, sh);
-      return v[0];
+    // Scalar evaluated on lane 0 of the calling warp and broadcast (binary64 transcendentals and
+    // divisions cost dozens of binary64 instructions each).
+    template <typename F>
+    __device__ inline double lane0(F&& f) {
+      double v = 0;
+      if ((threadIdx.x & 31) == 0) v = f();
+      return __shfl_sync(FULL, v, 0);
     }
 
     struct Ctx {
@@ -80,6 +78,11 @@ namespace flygpu {
       std::uint16_t* nbr;
       double* v;
       double const* hist;
+      std::uint8_t const* mob;
+      double* rho0;
+      std::uint16_t* need;
+      std::uint16_t* mnbr;
+      std::uint16_t* mcnt;
       double rc2;
       float rc2f;
       double L[3], invL[3];
@@ -157,11 +160,11 @@ namespace flygpu {
     template <int LPA>
     __device__ inline double lane_sum(double v) {
 #pragma unroll
-      for (int o = LPA / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o, LPA);
+      for (int o = LPA / 2; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o, LPA);
       return v;
     }
 
-    // ------------------------------------------------------------------ EAM passes
+    // ------------------------------------------------------------------ EAM passes (all threads)
 
     // Density pass over all atoms: F'(rho) into xl[i].w (and pk[i].fp). With ENERGY, accumulates
     // 0.5 * sum v + F(rho) into *e (per thread).
@@ -206,13 +209,13 @@ namespace flygpu {
               }
               if (++chunk == 8) {
                 rho += static_cast<double>(rf);
-                vs += static_cast<double>(vf);
+                if (ENERGY) vs += static_cast<double>(vf);
                 rf = vf = 0.f;
                 chunk = 0;
               }
             }
             rho += static_cast<double>(rf);
-            vs += static_cast<double>(vf);
+            if (ENERGY) vs += static_cast<double>(vf);
           } else {
             for (int k = l; k < cnt; k += LPA) {
               int const j = c.nbr[static_cast<std::int64_t>(k) * c.n + i];
@@ -358,18 +361,128 @@ namespace flygpu {
       }
     }
 
+    // Pair density term phi(t_j, t_i)(r_ij) of neighbour j at atom i: binary32 (MIXED) or binary64.
+    template <bool MIXED>
+    __device__ inline bool rho_term(Ctx const& c, TablesView const& tb, Packed const& me, int i, int ti, int j,
+                                    float& rf, double& rd) {
+      int const nty = tb.n_types;
+      if (MIXED) {
+        float dx, dy, dz;
+        dr32(c, me, i, j, dx, dy, dz);
+        float const r2 = dx * dx + dy * dy + dz * dz;
+        if (r2 < c.rc2f) {
+          int ii;
+          float tt;
+          if (!fetch32(sqrtf(r2), tb.finv_dR, tb.nR, ii, tt)) return false;
+          float4 const cp = __ldg(&tb.phi32[static_cast<std::int64_t>(c.ty[j] + nty * ti) * tb.nR + ii]);
+          rf += cp.x + tt * (cp.y + tt * (cp.z + tt * cp.w));
+        }
+      } else {
+        double dx, dy, dz;
+        dr64(c, i, j, dx, dy, dz);
+        double const r2 = (dx * dx + dy * dy) + dz * dz;
+        if (r2 < c.rc2) {
+          long long ii;
+          double x0;
+          if (!fetch64(sqrt(r2), tb.inv_dR, tb.dR, tb.nR, ii, x0)) return false;
+          D4 const cp = tb.phi64[static_cast<std::int64_t>(c.ty[j] + nty * ti) * tb.nR + ii];
+          rd += cp.x + x0 * (cp.y + x0 * (cp.z + x0 * cp.w));
+        }
+      }
+      return true;
+    }
+
+    // Density of every static atom from its static neighbours. Static atoms never move during a
+    // search, so this part of their density is fixed; computed once per search (all threads).
+    template <bool MIXED>
+    __device__ void static_density(Ctx const& c, TablesView const& tb, Blk& sh) {
+      for (int b = threadIdx.x; b < c.n; b += blockDim.x) {
+        if (c.mob[b]) continue;
+        Packed const me = c.pk[b];
+        int const tb_ = c.ty[b];
+        double rho = 0;
+        float rf = 0.f;
+        int const cnt = c.ncnt[b];
+        for (int k = 0; k < cnt; ++k) {
+          int const j = c.nbr[static_cast<std::int64_t>(k) * c.n + b];
+          if (c.mob[j]) continue;
+          if (!rho_term<MIXED>(c, tb, me, b, tb_, j, rf, rho)) atomicOr(&sh.flag, F_OOB);
+          if (MIXED && (k & 7) == 7) {
+            rho += static_cast<double>(rf);
+            rf = 0.f;
+          }
+        }
+        c.rho0[b] = rho + static_cast<double>(rf);
+      }
+    }
+
+    // Density pass of one gradient evaluation, over the needed atoms only: a mobile atom sums all its
+    // neighbours; a static atom adds its mobile neighbours' terms to its fixed static density.
     template <bool MIXED, int LPA>
-    __device__ void gradient(Ctx const& c, TablesView const& tb, Blk& sh, double* out) {
+    __device__ void density_inc(Ctx const& c, TablesView const& tb, Blk& sh) {
+      int const nt = blockDim.x;
+      int const total = sh.n_need * LPA;
+      int const rounds = (total + nt - 1) / nt;
+      for (int r = 0; r < rounds; ++r) {
+        int const t = r * nt + threadIdx.x;
+        bool const valid = t < total;
+        int const i = valid ? c.need[t / LPA] : 0;
+        int const l = t % LPA;
+        double rho = 0;
+        if (valid) {
+          int const ti = c.ty[i];
+          Packed const me = c.pk[i];
+          bool const m = c.mob[i] != 0;
+          int const cnt = m ? c.ncnt[i] : c.mcnt[i];
+          std::uint16_t const* list = m ? c.nbr : c.mnbr;
+          if (!m && l == 0) rho = c.rho0[i];
+          float rf = 0.f;
+          int chunk = 0;
+          for (int k = l; k < cnt; k += LPA) {
+            int const j = list[static_cast<std::int64_t>(k) * c.n + i];
+            if (!rho_term<MIXED>(c, tb, me, i, ti, j, rf, rho)) atomicOr(&sh.flag, F_OOB);
+            if (MIXED && ++chunk == 8) {
+              rho += static_cast<double>(rf);
+              rf = 0.f;
+              chunk = 0;
+            }
+          }
+          rho += static_cast<double>(rf);
+        }
+        rho = lane_sum<LPA>(rho);
+        if (valid && l == 0) {
+          int const ti = c.ty[i];
+          long long ii;
+          double x0;
+          double fp = 0;
+          if (fetch64(rho, tb.inv_dP, tb.dP, tb.nP, ii, x0)) {
+            D4 const cf = tb.F64[static_cast<std::int64_t>(ti) * tb.nP + ii];
+            fp = cf.y + x0 * (2.0 * cf.z + x0 * 3.0 * cf.w);
+          } else {
+            atomicOr(&sh.flag, F_OOB);
+          }
+          c.xl[i].w = fp;
+          if (MIXED) c.pk[i].fp = static_cast<float>(fp);
+        }
+      }
+    }
+
+    // One EAM gradient evaluation into out (mobile DOFs). Called by every thread; returns true when a
+    // device-side error was raised (the caller ends the search).
+    template <bool MIXED, int LPA>
+    __device__ bool gradient(Ctx const& c, TablesView const& tb, Blk& sh, double* out) {
       __syncthreads();
       if (MIXED) {
         for (int k = threadIdx.x; k < c.na; k += blockDim.x) pack_one(c, c.aatom[k]);
         __syncthreads();
       }
-      density<MIXED, LPA, false>(c, tb, sh, nullptr);
+      density_inc<MIXED, LPA>(c, tb, sh);
       __syncthreads();
       force<MIXED, LPA>(c, tb, sh, out);
       __syncthreads();
+      int const f = sh.flag;
       if (threadIdx.x == 0) c.S->grad_calls += 1;
+      return f != 0;
     }
 
     template <bool MIXED, int LPA>
@@ -379,23 +492,18 @@ namespace flygpu {
         for (int k = threadIdx.x; k < c.na; k += blockDim.x) pack_one(c, c.aatom[k]);
         __syncthreads();
       }
-      double e[1] = {0.0};
-      density<MIXED, LPA, true>(c, tb, sh, &e[0]);
-      bsum<1>(e, sh);
-      return e[0];
+      double e = 0.0;
+      density<MIXED, LPA, true>(c, tb, sh, &e);
+      return block_sum(e, sh);
     }
 
-    // ------------------------------------------------------------------ neighbour list
-
-    // List::update (list.cpp:37-51) on mobile atoms: xl -= d.
-    __device__ inline void list_update(Ctx const& c, double const* d) {
-      for (int e = threadIdx.x; e < c.M; e += blockDim.x) comp(c.xl[c.aatom[e / 3]], e % 3) -= d[e];
-    }
+    // ------------------------------------------------------------------ neighbour list (all threads)
 
     // List::rebuild (list.cpp:53-95): canonical images of the mobile positions, then every pair within
     // rc_list (plus a margin covering binary32 rounding) -- a superset of the reference's list, so the
-    // exact r < r_cut filter at evaluation time sees the same pairs.
-    __device__ void rebuild(Ctx const& c, Blk& sh, double rc_list) {
+    // exact r < r_cut filter at evaluation time sees the same pairs. Returns true on error.
+    __device__ bool rebuild(Ctx const& c, Blk& sh, double rc_list) {
+      __syncthreads();
       double const* X = c.V(V_X);
       for (int e = threadIdx.x; e < c.M; e += blockDim.x) {
         int const k = e % 3;
@@ -424,84 +532,127 @@ namespace flygpu {
         if (cnt > NB_CAP) atomicOr(&sh.flag, F_NLIST);
         c.ncnt[i] = static_cast<std::uint16_t>(min(cnt, NB_CAP));
       }
+      if (threadIdx.x == 0) sh.n_need = 0;
       __syncthreads();
+      // Needed atoms (mobile atoms and every neighbour of one) and each static one's mobile neighbours.
+      // The order of the needed list does not matter: each atom's density is computed independently.
+      for (int b = threadIdx.x; b < c.n; b += blockDim.x) {
+        bool const m = c.mob[b] != 0;
+        bool need = m;
+        int mc = 0;
+        if (!m) {
+          int const cnt = c.ncnt[b];
+          for (int k = 0; k < cnt; ++k) {
+            int const j = c.nbr[static_cast<std::int64_t>(k) * c.n + b];
+            if (c.mob[j]) c.mnbr[static_cast<std::int64_t>(mc++) * c.n + b] = static_cast<std::uint16_t>(j);
+          }
+          need = mc > 0;
+        }
+        c.mcnt[b] = static_cast<std::uint16_t>(mc);
+        if (need) c.need[atomicAdd(&sh.n_need, 1)] = static_cast<std::uint16_t>(b);
+      }
+      __syncthreads();
+      return sh.flag != 0;
     }
 
-    // ------------------------------------------------------------------ L-BFGS two-loop core
+    // ------------------------------------------------------------------ warp-0 vector algebra
 
-    // StepLBFGS::newton_step_impl (lbfgs_core.cpp:29-87) over the block's vectors.
-    // s(j) = s0 + j M and y(j) = y0 + j M hold the history; rho / alpha its scalars.
-    __device__ void newton(Ctx const& c, Blk& sh, int m, int& k, double* s0, double* y0, double* rho, double* alpha,
+    __device__ inline double wdot(double const* a, double const* b, int M) {
+      double s = 0;
+      for (int e = threadIdx.x; e < M; e += 32) s += a[e] * b[e];
+      return warp_sum(s);
+    }
+
+    // List::update (list.cpp:37-51) on mobile atoms: xl -= d (warp 0).
+    __device__ inline void wlist_update(Ctx const& c, double const* d, double sign) {
+      for (int e = threadIdx.x; e < c.M; e += 32) comp(c.xl[c.aatom[e / 3]], e % 3) -= sign * d[e];
+    }
+
+    // StepLBFGS::newton_step_impl (lbfgs_core.cpp:29-87), warp 0. s(j) = s0 + j M, y(j) = y0 + j M.
+    __device__ void newton(Ctx const& c, int m, int& k, double* s0, double* y0, double* rho, double* alpha,
                            double* px, double* pg, double const* x, double const* g, double* out) {
       int const M = c.M;
+      int const lane = threadIdx.x;
       auto S_ = [&](int j) { return s0 + static_cast<std::int64_t>(j) * M; };
       auto Y_ = [&](int j) { return y0 + static_cast<std::int64_t>(j) * M; };
       int const prev = k > 0 ? (k - 1) % m : 0;
       if (k > 0) {
         double* sp = S_(prev);
         double* yp = Y_(prev);
-        double d[1] = {0.0};
-        for (int e = threadIdx.x; e < M; e += blockDim.x) {
+        double d = 0;
+        for (int e = lane; e < M; e += 32) {
           sp[e] = x[e] - px[e];
           yp[e] = g[e] - pg[e];
-          d[0] += sp[e] * yp[e];
+          d += sp[e] * yp[e];
         }
-        bsum<1>(d, sh);
-        if (threadIdx.x == 0) rho[prev] = 1.0 / fabs(d[0]);
+        d = warp_sum(d);
+        double const r = lane0([&] { return 1.0 / fabs(d); });
+        if (lane == 0) rho[prev] = r;
       }
-      for (int e = threadIdx.x; e < M; e += blockDim.x) {
+      for (int e = lane; e < M; e += 32) {
         px[e] = x[e];
         pg[e] = g[e];
         out[e] = g[e];
       }
+      __syncwarp();
       int const incur = k <= m ? 0 : k - m;
       int const bound = k <= m ? k : m;
       for (int i = bound - 1; i >= 0; --i) {
         int const j = (i + incur) % m;
         double const* s = S_(j);
         double const* y = Y_(j);
-        double d[1] = {0.0};
-        for (int e = threadIdx.x; e < M; e += blockDim.x) d[0] += s[e] * out[e];
-        bsum<1>(d, sh);
-        double const a = rho[j] * d[0];
-        if (threadIdx.x == 0) alpha[j] = a;
-        for (int e = threadIdx.x; e < M; e += blockDim.x) out[e] -= a * y[e];
+        double const a = rho[j] * wdot(s, out, M);
+        if (lane == 0) alpha[j] = a;
+        for (int e = lane; e < M; e += 32) out[e] -= a * y[e];
       }
       if (k > 0) {
         double const* yp = Y_(prev);
-        double const yy = dot1(yp, yp, M, sh);
-        double const scale = 1.0 / rho[prev] / yy;
-        for (int e = threadIdx.x; e < M; e += blockDim.x) out[e] = out[e] * scale;
+        double const yy = wdot(yp, yp, M);
+        double const rp = rho[prev];
+        double const scale = lane0([&] { return 1.0 / rp / yy; });
+        for (int e = lane; e < M; e += 32) out[e] = out[e] * scale;
       }
+      __syncwarp();
       for (int i = 0; i <= bound - 1; ++i) {
         int const j = (i + incur) % m;
         double const* s = S_(j);
         double const* y = Y_(j);
-        double d[1] = {0.0};
-        for (int e = threadIdx.x; e < M; e += blockDim.x) d[0] += y[e] * out[e];
-        bsum<1>(d, sh);
-        double const beta = rho[j] * d[0];
+        double const beta = rho[j] * wdot(y, out, M);
         double const a = alpha[j];
-        for (int e = threadIdx.x; e < M; e += blockDim.x) out[e] += (a - beta) * s[e];
+        for (int e = lane; e < M; e += 32) out[e] += (a - beta) * s[e];
       }
+      __syncwarp();
       ++k;
     }
 
-    // trans_proj (rotor.cpp:33-47): remove the mean per component.
-    __device__ void trans_proj(Ctx const& c, Blk& sh, double* x) {
+    // trans_proj (rotor.cpp:33-47), warp 0: remove the mean per component.
+    __device__ void trans_proj(Ctx const& c, double* x) {
       double p[3] = {0.0, 0.0, 0.0};
-      for (int e = threadIdx.x; e < c.M; e += blockDim.x) p[e % 3] += x[e];
-      bsum<3>(p, sh);
-      double const inv = 1.0 / static_cast<double>(c.na);
+      for (int e = threadIdx.x; e < c.M; e += 32) p[e % 3] += x[e];
+      for (double& v : p) v = warp_sum(v);
+      double const inv = lane0([&] { return 1.0 / static_cast<double>(c.na); });
       double const q[3] = {p[0] * inv, p[1] * inv, p[2] * inv};
-      for (int e = threadIdx.x; e < c.M; e += blockDim.x) x[e] -= q[e % 3];
+      for (int e = threadIdx.x; e < c.M; e += 32) x[e] -= q[e % 3];
+      __syncwarp();
+    }
+
+    // Broadcast of warp 0's decision to the block.
+    __device__ inline int block_action(Blk& sh, int act) {
+      if (threadIdx.x == 0) sh.action = act;
+      __syncthreads();
+      int const a = sh.action;
+      __syncthreads();
+      return a;
     }
 
     // ------------------------------------------------------------------ Rotor::eff_gradient
 
+    // Returns true on a device-side error; the curvature lands in sh.curv.
     template <bool MIXED, int LPA>
-    __device__ double eff_gradient(Ctx const& c, TablesView const& tb, SearchOpts const& o, Blk& sh) {
+    __device__ bool eff_gradient(Ctx const& c, TablesView const& tb, SearchOpts const& o, Blk& sh) {
       int const M = c.M;
+      bool const lead = threadIdx.x < 32;
+      int const lane = threadIdx.x & 31;
       double* ax = c.V(V_AX);
       double* g0 = c.V(V_G0);
       double* g1 = c.V(V_G1);
@@ -512,84 +663,118 @@ namespace flygpu {
       double* eff = c.V(V_EFF);
       double const dr = o.delta_r;
       int kR = 0;
-      gradient<MIXED, LPA>(c, tb, sh, g0);
-      for (int e = threadIdx.x; e < M; e += blockDim.x) dprev[e] = -dr * ax[e];
-      list_update(c, dprev);
-      gradient<MIXED, LPA>(c, tb, sh, g1);
       double curv = 0;
-      for (int i = 0;; i++) {
-        double* dg = g1p;  // scratch until the trial gradient is evaluated
-        double t[1] = {0.0};
-        for (int e = threadIdx.x; e < M; e += blockDim.x) {
-          dg[e] = g1[e] - g0[e];
-          t[0] += dg[e] * ax[e];
-        }
-        bsum<1>(t, sh);
-        for (int e = threadIdx.x; e < M; e += blockDim.x) dg[e] -= t[0] * ax[e];
-        if (c.S->count_frozen == 0) trans_proj(c, sh, dg);
-        newton(c, sh, c.mR, kR, c.sR(0), c.yR(0), sh.rhoR, sh.alphaR, c.V(V_PXR), c.V(V_PGR), ax, dg, th);
-        double const tp = dot1(th, ax, M, sh);
-        double nn[1] = {0.0};
-        for (int e = threadIdx.x; e < M; e += blockDim.x) {
-          th[e] -= tp * ax[e];
-          nn[0] += th[e] * th[e];
-        }
-        bsum<1>(nn, sh);
-        double const inv = 1 / sqrt(nn[0]);
-        double bc[2] = {0.0, 0.0};
-        for (int e = threadIdx.x; e < M; e += blockDim.x) {
-          th[e] *= inv;
-          double const df = g1[e] - g0[e];
-          bc[0] += df * th[e];
-          bc[1] += df * ax[e];
-        }
-        bsum<2>(bc, sh);
-        double const b_1 = bc[0] / dr;
-        double const c_x0 = bc[1] / dr;
-        double const theta_1 = -0.5 * atan(b_1 / fabs(c_x0));
-        if (fabs(theta_1) < o.theta_tol || (i >= o.iter_max_rot && c_x0 < 0) || i > 10 * o.iter_max_rot) {
-          curv = c_x0;
-          break;
-        }
-        double const c1 = cos(theta_1), s1 = sin(theta_1);
-        for (int e = threadIdx.x; e < M; e += blockDim.x) {
-          axp[e] = ax[e] * c1 + th[e] * s1;
-          double const nd = -dr * axp[e];
-          double const upd = nd - dprev[e];
-          dprev[e] = nd;
-          comp(c.xl[c.aatom[e / 3]], e % 3) -= upd;
-        }
-        gradient<MIXED, LPA>(c, tb, sh, g1p);
-        double cx[1] = {0.0};
-        for (int e = threadIdx.x; e < M; e += blockDim.x) cx[0] += (g1p[e] - g0[e]) * axp[e];
-        bsum<1>(cx, sh);
-        double const c_x1 = cx[0] / dr;
-        double const a_1 = (c_x0 - c_x1 + b_1 * sin(2 * theta_1)) / (1 - cos(2 * theta_1));
-        double theta_min = 0.5 * atan(b_1 / a_1);
-        if (a_1 * cos(2 * theta_min) - a_1 + b_1 * sin(2 * theta_min) > 0) theta_min += M_PI / 2;
-        double const cm = cos(theta_min), sm = sin(theta_min);
-        double const w1 = sin(theta_1 - theta_min) / sin(theta_1);
-        double const w1p = sm / sin(theta_1);
-        double const w0 = 1 - cm - sm * tan(0.5 * theta_1);
-        for (int e = threadIdx.x; e < M; e += blockDim.x) {
-          ax[e] = ax[e] * cm + th[e] * sm;
-          g1[e] = w1 * g1[e] + w1p * g1p[e] + w0 * g0[e];
-        }
-        if (fabs(theta_min) < o.theta_tol) {
-          double q[1] = {0.0};
-          for (int e = threadIdx.x; e < M; e += blockDim.x) q[0] += (g1[e] - g0[e]) * ax[e];
-          bsum<1>(q, sh);
-          curv = q[0] / dr;
-          break;
-        }
+      if (gradient<MIXED, LPA>(c, tb, sh, g0)) return true;
+      if (lead) {
+        for (int e = lane; e < M; e += 32) dprev[e] = -dr * ax[e];
+        __syncwarp();
+        wlist_update(c, dprev, 1.0);
       }
-      for (int e = threadIdx.x; e < M; e += blockDim.x) comp(c.xl[c.aatom[e / 3]], e % 3) -= -dprev[e];
-      double const p = dot1(g0, ax, M, sh);
-      bool const parallel_only = !o.relax_in_convex && curv > 0;
-      for (int e = threadIdx.x; e < M; e += blockDim.x) eff[e] = parallel_only ? -p * ax[e] : g0[e] - 2 * p * ax[e];
-      if (c.S->count_frozen == 0) trans_proj(c, sh, eff);
+      if (gradient<MIXED, LPA>(c, tb, sh, g1)) return true;
+      for (int i = 0;; i++) {
+        // rotation plane and trial angle (warp 0)
+        double theta_1 = 0, b_1 = 0, c_x0 = 0;
+        int act = ACT_GO;
+        if (lead) {
+          double* dg = g1p;  // scratch until the trial gradient is evaluated
+          double t = 0;
+          for (int e = lane; e < M; e += 32) {
+            dg[e] = g1[e] - g0[e];
+            t += dg[e] * ax[e];
+          }
+          t = warp_sum(t);
+          for (int e = lane; e < M; e += 32) dg[e] -= t * ax[e];
+          __syncwarp();
+          if (c.S->count_frozen == 0) trans_proj(c, dg);
+          newton(c, c.mR, kR, c.sR(0), c.yR(0), sh.rhoR, sh.alphaR, c.V(V_PXR), c.V(V_PGR), ax, dg, th);
+          double const tp = wdot(th, ax, M);
+          double nn = 0;
+          for (int e = lane; e < M; e += 32) {
+            th[e] -= tp * ax[e];
+            nn += th[e] * th[e];
+          }
+          nn = warp_sum(nn);
+          double const inv = lane0([&] { return 1 / sqrt(nn); });
+          double b = 0, cc = 0;
+          for (int e = lane; e < M; e += 32) {
+            th[e] *= inv;
+            double const df = g1[e] - g0[e];
+            b += df * th[e];
+            cc += df * ax[e];
+          }
+          b = warp_sum(b);
+          cc = warp_sum(cc);
+          b_1 = lane0([&] { return b / dr; });
+          c_x0 = lane0([&] { return cc / dr; });
+          double const b1 = b_1, cx0 = c_x0;
+          theta_1 = lane0([&] { return -0.5 * atan(b1 / fabs(cx0)); });
+          if (fabs(theta_1) < o.theta_tol || (i >= o.iter_max_rot && c_x0 < 0) || i > 10 * o.iter_max_rot) {
+            curv = c_x0;
+            act = ACT_STOP;
+          } else {
+            double const t1 = theta_1;
+            double const c1 = lane0([&] { return cos(t1); });
+            double const s1 = lane0([&] { return sin(t1); });
+            for (int e = lane; e < M; e += 32) {
+              axp[e] = ax[e] * c1 + th[e] * s1;
+              double const nd = -dr * axp[e];
+              double const upd = nd - dprev[e];
+              dprev[e] = nd;
+              comp(c.xl[c.aatom[e / 3]], e % 3) -= upd;
+            }
+          }
+        }
+        if (block_action(sh, act) == ACT_STOP) break;
+        if (gradient<MIXED, LPA>(c, tb, sh, g1p)) return true;
+        if (lead) {
+          double cx = 0;
+          for (int e = lane; e < M; e += 32) cx += (g1p[e] - g0[e]) * axp[e];
+          cx = warp_sum(cx);
+          double const t1 = theta_1, b1 = b_1, cx0 = c_x0;
+          // the rotor's scalar trigonometry (rotor.cpp:120-134) on lane 0, broadcast as a block
+          double sc[6];
+          if (lane == 0) {
+            double const c_x1 = cx / dr;
+            double const a_1 = (cx0 - c_x1 + b1 * sin(2 * t1)) / (1 - cos(2 * t1));
+            double theta_min = 0.5 * atan(b1 / a_1);
+            if (a_1 * cos(2 * theta_min) - a_1 + b1 * sin(2 * theta_min) > 0) theta_min += M_PI / 2;
+            double const cm = cos(theta_min), sm = sin(theta_min);
+            sc[0] = cm;
+            sc[1] = sm;
+            sc[2] = sin(t1 - theta_min) / sin(t1);
+            sc[3] = sm / sin(t1);
+            sc[4] = 1 - cm - sm * tan(0.5 * t1);
+            sc[5] = theta_min;
+          }
+#pragma unroll
+          for (int q = 0; q < 6; ++q) sc[q] = __shfl_sync(FULL, lane == 0 ? sc[q] : 0.0, 0);
+          double const cm = sc[0], sm = sc[1], w1 = sc[2], w1p = sc[3], w0 = sc[4], theta_min = sc[5];
+          double q = 0;
+          for (int e = lane; e < M; e += 32) {
+            ax[e] = ax[e] * cm + th[e] * sm;
+            g1[e] = w1 * g1[e] + w1p * g1p[e] + w0 * g0[e];
+            q += (g1[e] - g0[e]) * ax[e];
+          }
+          __syncwarp();
+          if (fabs(theta_min) < o.theta_tol) {
+            q = warp_sum(q);
+            curv = lane0([&] { return q / dr; });
+            act = ACT_STOP;
+          }
+        }
+        if (block_action(sh, act) == ACT_STOP) break;
+      }
+      if (lead) {
+        wlist_update(c, dprev, -1.0);  // xl -= -dprev: back to the centre
+        double const p = wdot(g0, ax, M);
+        bool const parallel_only = !o.relax_in_convex && curv > 0;
+        for (int e = lane; e < M; e += 32) eff[e] = parallel_only ? -p * ax[e] : g0[e] - 2 * p * ax[e];
+        __syncwarp();
+        if (c.S->count_frozen == 0) trans_proj(c, eff);
+        if (lane == 0) sh.curv = curv;
+      }
       __syncthreads();
-      return curv;
+      return false;
     }
 
     // ------------------------------------------------------------------ one search
@@ -615,6 +800,11 @@ namespace flygpu {
       c.nbr = S->nbr;
       c.v = S->vec;
       c.hist = S->hist;
+      c.mob = S->mob;
+      c.rho0 = S->rho0;
+      c.need = S->need;
+      c.mnbr = S->mnbr;
+      c.mcnt = S->mcnt;
       c.rc2 = o.r_cut * o.r_cut;
       c.rc2f = static_cast<float>(c.rc2);
       c.periodic = S->periodic_any != 0;
@@ -631,24 +821,19 @@ namespace flygpu {
       double* eff = c.V(V_EFF);
       double* hg = c.V(V_HG);
       int const M = c.M;
-      if (threadIdx.x == 0) sh.flag = 0;
+      bool const lead = threadIdx.x < 32;
+      int const lane = threadIdx.x & 31;
+      if (threadIdx.x == 0) {
+        sh.flag = 0;
+        sh.n_need = S->n_need;
+      }
       __syncthreads();
 
+      // warp 0 holds the search's scalars
       int kT = S->kT, it = S->it;
       double trust = S->trust, acc = S->acc, convex = S->convex, curv = S->curv;
       int exit_code = FLYGPU_EXIT_UNINIT;
-      bool done = false;
-
-      auto failed = [&]() -> bool {
-        __syncthreads();
-        int const f = sh.flag;
-        __syncthreads();
-        if (f) {
-          if (threadIdx.x == 0) S->status = (f & F_NLIST) ? FLYGPU_NLIST_OVERFLOW : FLYGPU_SPLINE_OOB;
-          done = true;
-        }
-        return f != 0;
-      };
+      bool done = false, err = false;
 
       if (S->stage == STAGE_INIT) {
         for (int i = threadIdx.x; i < c.n; i += blockDim.x) {
@@ -658,118 +843,147 @@ namespace flygpu {
           p.z = p.z - c.L[2] * floor(p.z * c.invL[2]);
           pack_one(c, i);
         }
+        err = rebuild(c, sh, S->rc_list);
+        static_density<MIXED>(c, tb, sh);
         __syncthreads();
-        rebuild(c, sh, S->rc_list);
+        err = err || sh.flag != 0;
         kT = 0;
         it = 0;
         acc = 0;
         convex = 0;
         curv = 0;
-        if (!failed()) {
+        if (!err) {
           if (dimer) {
-            curv = eff_gradient<MIXED, LPA>(c, tb, o, sh);
+            err = eff_gradient<MIXED, LPA>(c, tb, o, sh);
+            curv = sh.curv;
             trust = o.min_trust;
           } else {
-            gradient<MIXED, LPA>(c, tb, sh, eff);
+            err = gradient<MIXED, LPA>(c, tb, sh, eff);
             trust = o.min_trust_l;
           }
-          failed();
         }
       }
 
       int const max_steps = dimer ? o.max_steps : o.iter_max_l;
       double const f2 = dimer ? o.f2norm : o.f2norm_l;
       int steps_here = 0;
-      while (!done) {
-        if (it >= max_steps) {
-          exit_code = dimer ? FLYGPU_EXIT_ITER_MAX : 1;
-          done = true;
-          break;
-        }
-        if (bv.budget > 0 && steps_here >= bv.budget) break;
-        double const mag = dot1(eff, eff, M, sh);
-        if (mag < f2 * f2) {
-          exit_code = dimer ? FLYGPU_EXIT_SUCCESS : 0;
-          done = true;
-          break;
-        }
-        if (dimer && convex >= o.convex_max) {
-          exit_code = FLYGPU_EXIT_CONVEX;
-          done = true;
-          break;
-        }
-        if (dimer && o.use_history && S->n_hist > 0 && it % o.hist_check_freq == 0) {
-          double ctheta = -1;
-          double const* im = c.V(V_INMIN);
-          bool hit = false;
-          for (int h = 0; h < S->n_hist; ++h) {
-            double const* sp = c.hist + static_cast<std::int64_t>(h) * M;
-            double q[3] = {0.0, 0.0, 0.0};
-            for (int e = threadIdx.x; e < M; e += blockDim.x) {
-              double const d1 = X[e] - im[e], d2 = sp[e] - im[e];
-              q[0] += d1 * d2;
-              q[1] += d2 * d2;
-              q[2] += d1 * d1;
-            }
-            bsum<3>(q, sh);
-            ctheta = fmax(ctheta, q[0] / (sqrt(q[1]) * sqrt(q[2])));
-            if (ctheta > cos(S->theta_tol_hist)) {
-              hit = true;
-              break;
-            }
-          }
-          if (hit) {
-            exit_code = FLYGPU_EXIT_COLLISION;
+      while (!err) {
+        int act = ACT_GO;
+        if (lead) {
+          if (it >= max_steps) {
+            exit_code = dimer ? FLYGPU_EXIT_ITER_MAX : 1;
             done = true;
-            break;
+            act = ACT_STOP;
+          } else if (bv.budget > 0 && steps_here >= bv.budget) {
+            act = ACT_STOP;
+          } else {
+            double const mag = wdot(eff, eff, M);
+            if (mag < f2 * f2) {
+              exit_code = dimer ? FLYGPU_EXIT_SUCCESS : 0;
+              done = true;
+              act = ACT_STOP;
+            } else if (dimer && convex >= o.convex_max) {
+              exit_code = FLYGPU_EXIT_CONVEX;
+              done = true;
+              act = ACT_STOP;
+            } else if (dimer && o.use_history && S->n_hist > 0 && it % o.hist_check_freq == 0) {
+              double ctheta = -1;
+              double const* im = c.V(V_INMIN);
+              for (int h = 0; h < S->n_hist; ++h) {
+                double const* sp = c.hist + static_cast<std::int64_t>(h) * M;
+                double q0 = 0, q1 = 0, q2 = 0;
+                for (int e = lane; e < M; e += 32) {
+                  double const d1 = X[e] - im[e], d2 = sp[e] - im[e];
+                  q0 += d1 * d2;
+                  q1 += d2 * d2;
+                  q2 += d1 * d1;
+                }
+                q0 = warp_sum(q0);
+                q1 = warp_sum(q1);
+                q2 = warp_sum(q2);
+                double const ct = ctheta;
+                ctheta = lane0([&] { return fmax(ct, q0 / (sqrt(q1) * sqrt(q2))); });
+                double const cth = ctheta;
+                if (lane0([&] { return cth > cos(S->theta_tol_hist) ? 1.0 : 0.0; }) != 0.0) {
+                  exit_code = FLYGPU_EXIT_COLLISION;
+                  done = true;
+                  act = ACT_STOP;
+                  break;
+                }
+              }
+            }
+          }
+          if (act == ACT_GO) {
+            newton(c, c.mT, kT, c.sT(0), c.yT(0), S->rhoT, S->alphaT, c.V(V_PXT), c.V(V_PGT), X, eff, hg);
+            double const nrm = wdot(hg, hg, M);
+            double const tr = trust;
+            double const sc = lane0([&] { return fmin(1.0, tr / sqrt(nrm)); });
+            double hh = 0;
+            for (int e = lane; e < M; e += 32) {
+              hg[e] *= sc;
+              hh += hg[e] * hg[e];
+              X[e] -= hg[e];
+            }
+            hh = warp_sum(hh);
+            acc += lane0([&] { return sqrt(hh); });
+            if (acc > 0.5 * skin) {
+              acc = 0;
+              act = ACT_REBUILD;
+            } else {
+              __syncwarp();
+              wlist_update(c, hg, 1.0);
+            }
           }
         }
-        newton(c, sh, c.mT, kT, c.sT(0), c.yT(0), S->rhoT, S->alphaT, c.V(V_PXT), c.V(V_PGT), X, eff, hg);
-        double const nrm = dot1(hg, hg, M, sh);
-        double const sc = fmin(1.0, trust / sqrt(nrm));
-        double hh[1] = {0.0};
-        for (int e = threadIdx.x; e < M; e += blockDim.x) {
-          hg[e] *= sc;
-          hh[0] += hg[e] * hg[e];
-          X[e] -= hg[e];
-        }
-        bsum<1>(hh, sh);
-        acc += sqrt(hh[0]);
-        if (acc > 0.5 * skin) {
-          rebuild(c, sh, S->rc_list);
-          acc = 0;
-          if (failed()) break;
-        } else {
-          list_update(c, hg);
+        act = block_action(sh, act);
+        if (act == ACT_STOP) break;
+        if (act == ACT_REBUILD && rebuild(c, sh, S->rc_list)) {
+          err = true;
+          break;
         }
         if (dimer) {
-          curv = eff_gradient<MIXED, LPA>(c, tb, o, sh);
-          convex = curv > 0 ? convex + 1 : 0;
-        } else {
-          gradient<MIXED, LPA>(c, tb, sh, eff);
+          if (eff_gradient<MIXED, LPA>(c, tb, o, sh)) {
+            err = true;
+            break;
+          }
+          curv = sh.curv;
+        } else if (gradient<MIXED, LPA>(c, tb, sh, eff)) {
+          err = true;
+          break;
         }
-        if (failed()) break;
-        double const proj = dot1(eff, hg, M, sh);
-        double const ptol = dimer ? o.proj_tol : o.proj_tol_l;
-        if (proj < -ptol) {
-          trust = fmax(dimer ? o.min_trust : o.min_trust_l, (dimer ? o.shrink_trust : o.shrink_trust_l) * trust);
-        } else if (proj > ptol) {
-          trust = fmin(dimer ? o.max_trust : o.max_trust_l, (dimer ? o.grow_trust : o.grow_trust_l) * trust);
+        if (lead) {
+          if (dimer) convex = curv > 0 ? convex + 1 : 0;
+          double const proj = wdot(eff, hg, M);
+          double const ptol = dimer ? o.proj_tol : o.proj_tol_l;
+          if (proj < -ptol) {
+            trust = fmax(dimer ? o.min_trust : o.min_trust_l, (dimer ? o.shrink_trust : o.shrink_trust_l) * trust);
+          } else if (proj > ptol) {
+            trust = fmin(dimer ? o.max_trust : o.max_trust_l, (dimer ? o.grow_trust : o.grow_trust_l) * trust);
+          }
         }
         ++it;
         ++steps_here;
       }
+      // warp 0's verdict for the whole block
+      if (threadIdx.x == 0) sh.action = (done ? 1 : 0) | (err ? 2 : 0);
+      __syncthreads();
+      int const verdict = sh.action;
+      __syncthreads();
+      done = (verdict & 1) != 0;
+      err = (verdict & 2) != 0;
+      if (err && threadIdx.x == 0) S->status = (sh.flag & F_NLIST) ? FLYGPU_NLIST_OVERFLOW : FLYGPU_SPLINE_OOB;
       double e_final = 0;
-      if (done && S->status == FLYGPU_OK) e_final = energy<MIXED, LPA>(c, tb, sh);
+      if (done && !err) e_final = energy<MIXED, LPA>(c, tb, sh);
       __syncthreads();
       if (threadIdx.x == 0) {
         S->kT = kT;
+        S->n_need = sh.n_need;
         S->it = it;
         S->trust = trust;
         S->acc = acc;
         S->convex = convex;
         S->curv = curv;
-        if (done) {
+        if (done || err) {
           S->stage = STAGE_DONE;
           S->exit_code = exit_code;
           S->energy = e_final;
@@ -853,6 +1067,16 @@ namespace flygpu {
     o += up(sizeof(std::uint16_t) * static_cast<std::size_t>(n));
     l.type = o;
     o += up(static_cast<std::size_t>(n));
+    l.mob = o;
+    o += up(static_cast<std::size_t>(n));
+    l.rho0 = o;
+    o += up(sizeof(double) * static_cast<std::size_t>(n));
+    l.need = o;
+    o += up(sizeof(std::uint16_t) * static_cast<std::size_t>(n));
+    l.mnbr = o;
+    o += up(sizeof(std::uint16_t) * static_cast<std::size_t>(n) * NB_CAP);
+    l.mcnt = o;
+    o += up(sizeof(std::uint16_t) * static_cast<std::size_t>(n));
     l.total = o;
     return l;
   }
@@ -866,6 +1090,11 @@ namespace flygpu {
     S.nbr = reinterpret_cast<std::uint16_t*>(base + l.nbr);
     S.vec = reinterpret_cast<double*>(base + l.vec);
     S.hist = reinterpret_cast<double const*>(base + l.hist);
+    S.mob = reinterpret_cast<std::uint8_t*>(base + l.mob);
+    S.rho0 = reinterpret_cast<double*>(base + l.rho0);
+    S.need = reinterpret_cast<std::uint16_t*>(base + l.need);
+    S.mnbr = reinterpret_cast<std::uint16_t*>(base + l.mnbr);
+    S.mcnt = reinterpret_cast<std::uint16_t*>(base + l.mcnt);
   }
 
   void search_gather(BatchView const& v, std::int64_t const* d_act3_off, double* out_x, double* out_ax,
@@ -882,7 +1111,8 @@ namespace flygpu {
   }
 
   void search_launch(BatchView const& v, int lanes_per_atom, int threads, int blocks, bool mixed, cudaStream_t s) {
-    if (threads % 32 != 0 || threads < 32 || threads > 1024) fail(FLYGPU_INVALID_ARG, "threads must be 32..1024, multiple of 32");
+    if (threads % 32 != 0 || threads < 64 || threads > 1024)
+      fail(FLYGPU_INVALID_ARG, "threads must be 64..1024, a multiple of 32");
     if (mixed) {
       launch_lpa<true>(v, lanes_per_atom, threads, blocks, s);
     } else {

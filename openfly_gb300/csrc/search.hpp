@@ -65,6 +65,12 @@ namespace flygpu {
     std::uint16_t* nbr;     // [NB_CAP][n]
     double* vec;            // (N_VEC + 2 mT + 2 mR) vectors of 3 na doubles
     double const* hist;     // n_hist vectors of 3 na doubles (previous saddle points)
+    std::uint8_t* mob;      // per atom: 1 if it can move (mobile), else 0
+    double* rho0;           // per static atom: density from its static neighbours (fixed for the search)
+    std::uint16_t* need;    // atoms whose F' the force pass reads (mobile atoms and their neighbours)
+    std::uint16_t* mnbr;    // [NB_CAP][n]: mobile neighbours of each needed static atom
+    std::uint16_t* mcnt;    // per atom: count in mnbr
+    int n_need, pad2;
     double trust, acc, convex, curv, energy;
     std::int64_t grad_calls;
     double rhoT[MAX_HIST], alphaT[MAX_HIST];
@@ -84,7 +90,7 @@ namespace flygpu {
 
   // Byte offsets of one search's arrays inside its block (256-byte aligned parts).
   struct SearchLayout {
-    std::size_t xl, pk, type, aatom, ncnt, nbr, vec, hist, total;
+    std::size_t xl, pk, type, aatom, ncnt, nbr, vec, hist, mob, rho0, need, mnbr, mcnt, total;
   };
 
   // search.cu

@@ -228,6 +228,9 @@ namespace flygpu {
     int* aat = reinterpret_cast<int*>(base + l.aatom);
     double* v = reinterpret_cast<double*>(base + l.vec);
     double* h = reinterpret_cast<double*>(base + l.hist);
+    std::uint8_t* mb = reinterpret_cast<std::uint8_t*>(base + l.mob);
+    std::fill_n(mb, n, std::uint8_t{0});
+    for (int a : mob) mb[a] = 1;
     for (int i = 0; i < n; ++i) {
       xl[i] = D4{d.pos[3 * i], d.pos[3 * i + 1], d.pos[3 * i + 2], 0.0};
       ty[i] = static_cast<std::uint8_t>(d.types[i]);
