@@ -416,29 +416,32 @@ namespace flygpu {
       }
     }
 
-    // Density pass of one gradient evaluation, over the needed atoms only: a mobile atom sums all its
-    // neighbours; a static atom adds its mobile neighbours' terms to its fixed static density.
-    template <bool MIXED, int LPA>
+    // Density pass of one gradient evaluation over the atoms whose F' the force pass reads: each mobile
+    // atom with a group of W lanes over all its neighbours, then each needed static atom with one lane,
+    // adding its mobile neighbours' terms to its fixed static density.
+    template <bool MIXED, int W>
     __device__ void density_inc(Ctx const& c, TablesView const& tb, Blk& sh) {
       int const nt = blockDim.x;
-      int const total = sh.n_need * LPA;
+      int const nm = c.na * W;
+      int const total = nm + sh.n_need;
       int const rounds = (total + nt - 1) / nt;
       for (int r = 0; r < rounds; ++r) {
         int const t = r * nt + threadIdx.x;
         bool const valid = t < total;
-        int const i = valid ? c.need[t / LPA] : 0;
-        int const l = t % LPA;
+        bool const mobile = t < nm;
+        int const i = mobile ? c.aatom[t / W] : (valid ? c.need[t - nm] : 0);
+        int const l = mobile ? t % W : 0;
+        int const step = mobile ? W : 1;
         double rho = 0;
         if (valid) {
           int const ti = c.ty[i];
           Packed const me = c.pk[i];
-          bool const m = c.mob[i] != 0;
-          int const cnt = m ? c.ncnt[i] : c.mcnt[i];
-          std::uint16_t const* list = m ? c.nbr : c.mnbr;
-          if (!m && l == 0) rho = c.rho0[i];
+          int const cnt = mobile ? c.ncnt[i] : c.mcnt[i];
+          std::uint16_t const* list = mobile ? c.nbr : c.mnbr;
+          if (!mobile) rho = c.rho0[i];
           float rf = 0.f;
           int chunk = 0;
-          for (int k = l; k < cnt; k += LPA) {
+          for (int k = l; k < cnt; k += step) {
             int const j = list[static_cast<std::int64_t>(k) * c.n + i];
             if (!rho_term<MIXED>(c, tb, me, i, ti, j, rf, rho)) atomicOr(&sh.flag, F_OOB);
             if (MIXED && ++chunk == 8) {
@@ -449,7 +452,8 @@ namespace flygpu {
           }
           rho += static_cast<double>(rf);
         }
-        rho = lane_sum<LPA>(rho);
+        double const tot = lane_sum<W>(rho);
+        if (mobile) rho = tot;
         if (valid && l == 0) {
           int const ti = c.ty[i];
           long long ii;
@@ -467,6 +471,22 @@ namespace flygpu {
       }
     }
 
+    // Lanes per mobile atom in the EAM passes: the widest power of two (at least LPA, at most 32) that
+    // keeps the mobile atoms within one round of the block.
+    template <int LPA>
+    __device__ inline int wide_lanes(int na) {
+      int w = 32;
+      while (w > LPA && na * w > static_cast<int>(blockDim.x)) w >>= 1;
+      return w;
+    }
+
+    template <bool MIXED, int W>
+    __device__ void passes(Ctx const& c, TablesView const& tb, Blk& sh, double* out) {
+      density_inc<MIXED, W>(c, tb, sh);
+      __syncthreads();
+      force<MIXED, W>(c, tb, sh, out);
+    }
+
     // One EAM gradient evaluation into out (mobile DOFs). Called by every thread; returns true when a
     // device-side error was raised (the caller ends the search).
     template <bool MIXED, int LPA>
@@ -476,9 +496,14 @@ namespace flygpu {
         for (int k = threadIdx.x; k < c.na; k += blockDim.x) pack_one(c, c.aatom[k]);
         __syncthreads();
       }
-      density_inc<MIXED, LPA>(c, tb, sh);
-      __syncthreads();
-      force<MIXED, LPA>(c, tb, sh, out);
+      switch (wide_lanes<LPA>(c.na)) {
+        case 32: passes<MIXED, 32>(c, tb, sh, out); break;
+        case 16: passes<MIXED, 16>(c, tb, sh, out); break;
+        case 8: passes<MIXED, (LPA > 8 ? LPA : 8)>(c, tb, sh, out); break;
+        case 4: passes<MIXED, (LPA > 4 ? LPA : 4)>(c, tb, sh, out); break;
+        case 2: passes<MIXED, (LPA > 2 ? LPA : 2)>(c, tb, sh, out); break;
+        default: passes<MIXED, LPA>(c, tb, sh, out); break;
+      }
       __syncthreads();
       int const f = sh.flag;
       if (threadIdx.x == 0) c.S->grad_calls += 1;
@@ -502,6 +527,8 @@ namespace flygpu {
     // List::rebuild (list.cpp:53-95): canonical images of the mobile positions, then every pair within
     // rc_list (plus a margin covering binary32 rounding) -- a superset of the reference's list, so the
     // exact r < r_cut filter at evaluation time sees the same pairs. Returns true on error.
+    __device__ void static_lists(Ctx const& c, Blk& sh, double rc_list);
+
     __device__ bool rebuild(Ctx const& c, Blk& sh, double rc_list) {
       __syncthreads();
       double const* X = c.V(V_X);
@@ -532,26 +559,87 @@ namespace flygpu {
         if (cnt > NB_CAP) atomicOr(&sh.flag, F_NLIST);
         c.ncnt[i] = static_cast<std::uint16_t>(min(cnt, NB_CAP));
       }
+      static_lists(c, sh, rc_list);
+      return sh.flag != 0;
+    }
+
+    // Static atoms with a mobile neighbour ("needed": the force pass reads their F') and each one's
+    // mobile neighbours, in mobile-index order. The order of the needed list itself does not matter.
+    __device__ void static_lists(Ctx const& c, Blk& sh, double rc_list) {
+      float const lim = static_cast<float>((rc_list + 1e-3) * (rc_list + 1e-3));
       if (threadIdx.x == 0) sh.n_need = 0;
       __syncthreads();
-      // Needed atoms (mobile atoms and every neighbour of one) and each static one's mobile neighbours.
-      // The order of the needed list does not matter: each atom's density is computed independently.
       for (int b = threadIdx.x; b < c.n; b += blockDim.x) {
-        bool const m = c.mob[b] != 0;
-        bool need = m;
+        if (c.mob[b]) continue;
+        Packed const me = c.pk[b];
         int mc = 0;
-        if (!m) {
-          int const cnt = c.ncnt[b];
-          for (int k = 0; k < cnt; ++k) {
-            int const j = c.nbr[static_cast<std::int64_t>(k) * c.n + b];
-            if (c.mob[j]) c.mnbr[static_cast<std::int64_t>(mc++) * c.n + b] = static_cast<std::uint16_t>(j);
+        for (int k = 0; k < c.na; ++k) {
+          int const a = c.aatom[k];
+          Packed const o = c.pk[a];
+          float dx = o.hx - me.hx, dy = o.hy - me.hy, dz = o.hz - me.hz;
+          if (c.periodic) {
+            if (c.per[0]) dx -= c.Lf[0] * rintf(dx / c.Lf[0]);
+            if (c.per[1]) dy -= c.Lf[1] * rintf(dy / c.Lf[1]);
+            if (c.per[2]) dz -= c.Lf[2] * rintf(dz / c.Lf[2]);
           }
-          need = mc > 0;
+          if (dx * dx + dy * dy + dz * dz < lim) {
+            if (mc < NB_CAP) c.mnbr[static_cast<std::int64_t>(mc) * c.n + b] = static_cast<std::uint16_t>(a);
+            ++mc;
+          }
         }
-        c.mcnt[b] = static_cast<std::uint16_t>(mc);
-        if (need) c.need[atomicAdd(&sh.n_need, 1)] = static_cast<std::uint16_t>(b);
+        if (mc > NB_CAP) atomicOr(&sh.flag, F_NLIST);
+        c.mcnt[b] = static_cast<std::uint16_t>(min(mc, NB_CAP));
+        if (mc > 0) c.need[atomicAdd(&sh.n_need, 1)] = static_cast<std::uint16_t>(b);
       }
       __syncthreads();
+    }
+
+    // Rebuild after a translation step: static atoms never move, so static-static pairs never change.
+    // Only the mobile atoms' lists (one warp per mobile atom, in atom order) and the static atoms'
+    // mobile-neighbour lists are rebuilt. Returns true on error.
+    __device__ bool rebuild_mobile(Ctx const& c, Blk& sh, double rc_list) {
+      __syncthreads();
+      double const* X = c.V(V_X);
+      for (int e = threadIdx.x; e < c.M; e += blockDim.x) {
+        int const k = e % 3;
+        comp(c.xl[c.aatom[e / 3]], k) = X[e] - c.L[k] * floor(X[e] * c.invL[k]);
+      }
+      __syncthreads();
+      for (int k = threadIdx.x; k < c.na; k += blockDim.x) pack_one(c, c.aatom[k]);
+      __syncthreads();
+      float const lim = static_cast<float>((rc_list + 1e-3) * (rc_list + 1e-3));
+      int const lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+      for (int k = threadIdx.x >> 5; k < c.na; k += nw) {
+        int const i = c.aatom[k];
+        Packed const me = c.pk[i];
+        int cnt = 0;
+        for (int j0 = 0; j0 < c.n; j0 += 32) {
+          int const j = j0 + lane;
+          bool hit = false;
+          if (j < c.n && j != i) {
+            Packed const o = c.pk[j];
+            float dx = o.hx - me.hx, dy = o.hy - me.hy, dz = o.hz - me.hz;
+            if (c.periodic) {
+              if (c.per[0]) dx -= c.Lf[0] * rintf(dx / c.Lf[0]);
+              if (c.per[1]) dy -= c.Lf[1] * rintf(dy / c.Lf[1]);
+              if (c.per[2]) dz -= c.Lf[2] * rintf(dz / c.Lf[2]);
+            }
+            hit = dx * dx + dy * dy + dz * dz < lim;
+          }
+          unsigned const mask = __ballot_sync(FULL, hit);
+          if (hit) {
+            int const p = cnt + __popc(mask & ((1u << lane) - 1u));
+            if (p < NB_CAP) c.nbr[static_cast<std::int64_t>(p) * c.n + i] = static_cast<std::uint16_t>(j);
+          }
+          cnt += __popc(mask);
+        }
+        if (lane == 0) {
+          if (cnt > NB_CAP) atomicOr(&sh.flag, F_NLIST);
+          c.ncnt[i] = static_cast<std::uint16_t>(min(cnt, NB_CAP));
+        }
+      }
+      __syncthreads();
+      static_lists(c, sh, rc_list);
       return sh.flag != 0;
     }
 
@@ -707,14 +795,26 @@ namespace flygpu {
           b_1 = lane0([&] { return b / dr; });
           c_x0 = lane0([&] { return cc / dr; });
           double const b1 = b_1, cx0 = c_x0;
-          theta_1 = lane0([&] { return -0.5 * atan(b1 / fabs(cx0)); });
+          if (MIXED) {  // rotation angles in binary32 (see rotor_angles)
+            theta_1 = -0.5 * static_cast<double>(atanf(static_cast<float>(b1) / fabsf(static_cast<float>(cx0))));
+          } else {
+            theta_1 = lane0([&] { return -0.5 * atan(b1 / fabs(cx0)); });
+          }
           if (fabs(theta_1) < o.theta_tol || (i >= o.iter_max_rot && c_x0 < 0) || i > 10 * o.iter_max_rot) {
             curv = c_x0;
             act = ACT_STOP;
           } else {
             double const t1 = theta_1;
-            double const c1 = lane0([&] { return cos(t1); });
-            double const s1 = lane0([&] { return sin(t1); });
+            double c1, s1;
+            if (MIXED) {
+              float sf, cf;
+              sincosf(static_cast<float>(t1), &sf, &cf);
+              c1 = cf;
+              s1 = sf;
+            } else {
+              c1 = lane0([&] { return cos(t1); });
+              s1 = lane0([&] { return sin(t1); });
+            }
             for (int e = lane; e < M; e += 32) {
               axp[e] = ax[e] * c1 + th[e] * s1;
               double const nd = -dr * axp[e];
@@ -733,7 +833,30 @@ namespace flygpu {
           double const t1 = theta_1, b1 = b_1, cx0 = c_x0;
           // the rotor's scalar trigonometry (rotor.cpp:120-134) on lane 0, broadcast as a block
           double sc[6];
-          if (lane == 0) {
+          if (MIXED) {
+            // Rotor angles in binary32: the curvatures c_x0, c_x1 and b_1 come from binary64 dots; the
+            // angle arithmetic of rotor.cpp:120-134 is carried in binary32 (errors ~1e-7 rad, far below
+            // the rotor's angle tolerance), with 1 - cos(2x) written as 2 sin^2(x) to keep its precision.
+            double const c_x1 = cx / dr;
+            float const f1 = static_cast<float>(t1);
+            float s1f, c1f, s2f, c2f;
+            sincosf(f1, &s1f, &c1f);
+            sincosf(2.f * f1, &s2f, &c2f);
+            double const a_1 = (cx0 - c_x1 + b1 * static_cast<double>(s2f)) / (2.0 * static_cast<double>(s1f) * static_cast<double>(s1f));
+            float tm = 0.5f * atanf(static_cast<float>(b1 / a_1));
+            float sm2, cm2;
+            sincosf(2.f * tm, &sm2, &cm2);
+            float const sm1 = sinf(tm);
+            if (-2.0 * a_1 * static_cast<double>(sm1) * static_cast<double>(sm1) + b1 * static_cast<double>(sm2) > 0) tm += 1.57079632679489661923f;
+            float smf, cmf;
+            sincosf(tm, &smf, &cmf);
+            sc[0] = cmf;
+            sc[1] = smf;
+            sc[2] = sinf(f1 - tm) / s1f;
+            sc[3] = smf / s1f;
+            sc[4] = 1.0 - static_cast<double>(cmf) - static_cast<double>(smf) * static_cast<double>(tanf(0.5f * f1));
+            sc[5] = tm;
+          } else if (lane == 0) {
             double const c_x1 = cx / dr;
             double const a_1 = (cx0 - c_x1 + b1 * sin(2 * t1)) / (1 - cos(2 * t1));
             double theta_min = 0.5 * atan(b1 / a_1);
@@ -746,8 +869,10 @@ namespace flygpu {
             sc[4] = 1 - cm - sm * tan(0.5 * t1);
             sc[5] = theta_min;
           }
+          if (!MIXED) {
 #pragma unroll
-          for (int q = 0; q < 6; ++q) sc[q] = __shfl_sync(FULL, lane == 0 ? sc[q] : 0.0, 0);
+            for (int q = 0; q < 6; ++q) sc[q] = __shfl_sync(FULL, lane == 0 ? sc[q] : 0.0, 0);
+          }
           double const cm = sc[0], sm = sc[1], w1 = sc[2], w1p = sc[3], w0 = sc[4], theta_min = sc[5];
           double q = 0;
           for (int e = lane; e < M; e += 32) {
@@ -937,7 +1062,7 @@ namespace flygpu {
         }
         act = block_action(sh, act);
         if (act == ACT_STOP) break;
-        if (act == ACT_REBUILD && rebuild(c, sh, S->rc_list)) {
+        if (act == ACT_REBUILD && rebuild_mobile(c, sh, S->rc_list)) {
           err = true;
           break;
         }
@@ -973,7 +1098,14 @@ namespace flygpu {
       err = (verdict & 2) != 0;
       if (err && threadIdx.x == 0) S->status = (sh.flag & F_NLIST) ? FLYGPU_NLIST_OVERFLOW : FLYGPU_SPLINE_OOB;
       double e_final = 0;
-      if (done && !err) e_final = energy<MIXED, LPA>(c, tb, sh);
+      if (done && !err) {
+        // the energy sums every pair, so static atoms' lists must see the mobile atoms' final places
+        if (rebuild(c, sh, S->rc_list)) {
+          if (threadIdx.x == 0) S->status = FLYGPU_NLIST_OVERFLOW;
+        } else {
+          e_final = energy<MIXED, LPA>(c, tb, sh);
+        }
+      }
       __syncthreads();
       if (threadIdx.x == 0) {
         S->kT = kT;
