@@ -451,7 +451,7 @@ def main():
     ap.add_argument("--no-searches", action="store_true", help="skip the search metrics (configs 3 and 4)")
     ap.add_argument("--searches", type=int, default=4096, help="clusters in the batched search run")
     ap.add_argument("--plain-sample", type=int, default=32, help="searches timed on the plain path")
-    ap.add_argument("--arrival-rate", type=float, default=1500.0, help="served requests per second (Poisson)")
+    ap.add_argument("--arrival-rate", type=float, default=3000.0, help="served requests per second (Poisson)")
     ap.add_argument("--steps-per-tick", type=int, default=8, help="translation steps per serving tick")
     args = ap.parse_args()
     if args.warmup < 3:
