@@ -286,6 +286,42 @@ class Server:
         return {k: getattr(st, k) for k, _ in st._fields_}
 
 
+def pathways(eam: EAM, saddles: list[Search], minima: list[np.ndarray], precision: int = MIXED,
+             nudge_frac: float = 0.01, lbfgs: LBFGSOptions | None = None, tuning: Tuning | None = None):
+    """Master::do_adj_min (find.cpp:1014-1090) for many saddles at once: each saddle (positions = the
+    converged dimer, axis = its final axis) is nudged by +/- nudge_frac of its distance from the initial
+    minimum along the axis and both nudged states are relaxed with LBFGS::minimise, all in one batched
+    launch. As the reference, the relaxed state nearer the initial minimum is 'rev'. Returns one dict per
+    saddle: rev, fwd (n,3), E_rev, E_fwd, E_sp, barrier = E_sp - E_rev, and the minimisers' exit codes
+    (0 = converged). Clusters with frozen atoms need no translation freeze or drift correction; for a
+    fully mobile system the caller freezes one far atom first, as find.cpp:1026-1034 does."""
+    reqs = []
+    for s, x0 in zip(saddles, minima):
+        x = np.asarray(s.pos, np.float64).reshape(-1, 3)
+        ax = np.asarray(s.axis, np.float64).reshape(-1, 3)
+        disp = np.linalg.norm(x - np.asarray(x0).reshape(-1, 3))
+        for sign in (1.0, -1.0):
+            reqs.append(Search(x + sign * ax * disp * nudge_frac, s.types, s.frozen, s.extents, s.periodic,
+                               mode=MINIMISE))
+    b = Batch(eam, reqs, precision=precision, lbfgs=lbfgs)
+    b.run(tuning)
+    res, pos, _ = b.results()
+    sp = Batch(eam, [Search(s.pos, s.types, s.frozen, s.extents, s.periodic, mode=MINIMISE) for s in saddles],
+               precision=precision, lbfgs=LBFGSOptions.defaults(iter_max=0))
+    sp.run(tuning)
+    e_sp = [r["energy"] for r in sp.results(positions=False)[0]]
+    out = []
+    for k, x0 in enumerate(minima):
+        fwd, rev = pos[2 * k], pos[2 * k + 1]
+        rf, rr = res[2 * k], res[2 * k + 1]
+        x0 = np.asarray(x0).reshape(-1, 3)
+        if np.linalg.norm(rev - x0) > np.linalg.norm(fwd - x0):  # find.cpp:1054-1058
+            fwd, rev, rf, rr = rev, fwd, rr, rf
+        out.append(dict(rev=rev, fwd=fwd, E_rev=rr["energy"], E_fwd=rf["energy"], E_sp=e_sp[k],
+                        barrier=e_sp[k] - rr["energy"], exit_rev=rr["exit_code"], exit_fwd=rf["exit_code"]))
+    return out
+
+
 def search_plain(eam: EAM, s: Search, precision: int = FP64, dimer: DimerOptions | None = None,
                  lbfgs: LBFGSOptions | None = None):
     """One search the drop-in way; returns (result dict, positions (n,3), axis (n,3))."""

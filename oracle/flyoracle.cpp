@@ -1104,4 +1104,24 @@ void orc_xoshiro(std::uint64_t const* seed, std::uint64_t* out, long n) {
 
 int orc_max_threads() { return omp_get_max_threads(); }
 
+// AdjacentCells (neigh/adjacent.hpp:40-70) of one cell of a grid of the given shape; returns the count.
+int orc_adjacent(int const* shape, int cell, int* out) {
+  orc::Grid g(orc::Box(std::array<double, 3>{10, 10, 10}.data(), std::array<int, 3>{0, 0, 0}.data()), 1.0);
+  for (int k = 0; k < 3; ++k) g.shape[k] = shape[k];
+  g.prod[0] = 1;
+  g.prod[1] = shape[0];
+  g.prod[2] = shape[0] * shape[1];
+  auto adj = orc::adjacent_cells(g);
+  auto const& v = adj[static_cast<std::size_t>(cell)];
+  std::copy(v.begin(), v.end(), out);
+  return static_cast<int>(v.size());
+}
+
+// HyperGrid(extents, r_cut).cell_idx(x) (system/boxes/hypergrid.hpp:43-99).
+int orc_cell_idx(double const* ext, double r_cut, double const* x) {
+  int const per[3] = {0, 0, 0};
+  orc::Grid g(orc::Box(ext, per), r_cut);
+  return g.cell_idx(x);
+}
+
 }  // extern "C"

@@ -125,6 +125,8 @@ def lib() -> C.CDLL:
                                       C.c_int, _ip, _ip]
         L.orc_xoshiro.argtypes = [_u64p, _u64p, C.c_long]
         L.orc_max_threads.restype = C.c_int
+        L.orc_adjacent.argtypes = [_ip, C.c_int, _ip]
+        L.orc_cell_idx.argtypes = [_dp, C.c_double, _dp]
         _lib = L
     return _lib
 
@@ -325,3 +327,16 @@ def dimer_batch(data: EAMData, opt: DimerOptions, offsets, extents, periodic, po
 
 def max_threads() -> int:
     return lib().orc_max_threads()
+
+
+def adjacent(shape, cell: int) -> list[int]:
+    """AdjacentCells (neigh/adjacent.hpp:40-70) of one cell."""
+    out = np.zeros(26, dtype=np.int32)
+    n = lib().orc_adjacent(np.ascontiguousarray(shape, dtype=np.int32), cell, out)
+    return out[:n].tolist()
+
+
+def cell_idx(extents, r_cut: float, x) -> int:
+    """HyperGrid(extents, r_cut).cell_idx(x) (system/boxes/hypergrid.hpp:43-99)."""
+    return lib().orc_cell_idx(np.ascontiguousarray(extents, dtype=np.float64), r_cut,
+                              np.ascontiguousarray(x, dtype=np.float64))

@@ -1,4 +1,7 @@
 """The oracle against the reference's own known answers (CPU only)."""
+import json
+import os
+
 import numpy as np
 import pytest
 
@@ -96,6 +99,38 @@ def test_list_update_vs_brute_force(oracle):
         for (ia, da), (ib, db) in zip(a, b):
             assert np.array_equal(ia, ib)
             assert np.all(np.linalg.norm(da - db, axis=1) < 1e-9)
+
+
+KATS = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "reference_kats.json")))
+
+
+def test_golden_fixture_values(oracle, odata):
+    # tests/golden/reference_kats.json holds the values tests/golden/make_golden.py read out of the
+    # reference's test sources; the oracle reproduces each.
+    for x, fx in KATS["f_Fe"]:
+        assert near(odata.spline(0, 0, 0, 0, x), fx)
+    s = W.kat_lattice()
+    nl = oracle.List(s.extents, s.periodic, odata.r_cut)
+    nl.rebuild(s.pos, 2)
+    assert near(oracle.eam_energy(odata, nl, s.types, 2), KATS["E0"])
+    g = oracle.eam_gradient(odata, nl, s.types, s.frozen, 2)
+    assert np.linalg.norm(g[0] - KATS["grad0_component"]) < KATS["grad0_tol"]
+
+
+def test_adjacent_cells_kat(oracle):
+    # tests/neigh/adjacent.cpp:23-95
+    a = KATS["adjacent_5cubed"]
+    assert oracle.adjacent([5, 5, 5], a["interior_cell"]) == a["interior"]
+    assert len(oracle.adjacent([5, 5, 5], a["face_cell"])) == a["face_count"]
+    assert len(oracle.adjacent([5, 5, 5], a["edge_cell"])) == a["edge_count"]
+    assert len(oracle.adjacent([5, 5, 5], a["corner_cell"])) == a["corner_count"]
+
+
+def test_hypergrid_cell_idx_kat(oracle):
+    # tests/system/boxes/hypergrid.cpp:24-44
+    h = KATS["hypergrid_10_rc3"]
+    for k, x in h["x"].items():
+        assert oracle.cell_idx([10.0, 10.0, 10.0], 3.0, [x, x, x]) == h["idx"][k]
 
 
 def test_ghost_capacity_and_spline_oob(oracle, odata):

@@ -147,6 +147,36 @@ def test_config1_periodic_search(gpu, oracle, odata, geam, search_mod):
             assert abs(r["energy"] - ref["energy"]) < E_TOL
 
 
+def test_pathways_match_oracle(gpu, oracle, odata, geam, search_mod, clusters):
+    # Master::do_adj_min (find.cpp:1014-1090): minima either side of converged saddles, vs the oracle's
+    # LBFGS::minimise from the same nudged starting points; saddle energy vs the oracle's EAM::energy.
+    S, O = search_mod, oracle
+    gopt, _ = c3_options(S, O)
+    b = S.Batch(geam, [S.from_cluster(c) for c in clusters], precision=gpu.FP64, dimer=gopt)
+    b.run(S.Tuning(4, 128, 2))
+    res, pos, ax = b.results()
+    ok = [k for k, r in enumerate(res) if r["exit_code"] == 0][:5]
+    assert ok
+    sads = [S.Search(pos[k], clusters[k].sys.types, clusters[k].sys.frozen, clusters[k].sys.extents,
+                     clusters[k].sys.periodic, axis=ax[k]) for k in ok]
+    starts = [clusters[k].sys.pos for k in ok]
+    lopt = S.LBFGSOptions.defaults(f2norm=1e-4)
+    olopt = O.LBFGSOptions.defaults(f2norm=1e-4)
+    paths = S.pathways(geam, sads, starts, precision=gpu.FP64, lbfgs=lopt)
+    for k, p in zip(ok, paths):
+        s = clusters[k].sys
+        assert abs(p["E_sp"] - oracle_energy(O, odata, s, pos[k])) < 1e-6
+        disp = np.linalg.norm(pos[k] - s.pos)
+        ref = []
+        for sign in (1.0, -1.0):
+            x = pos[k] + sign * ax[k] * disp * 0.01
+            failed, _, xm, _ = O.lbfgs_minimise(odata, olopt, s.extents, s.periodic, x, s.types, s.frozen)
+            ref.append(oracle_energy(O, odata, s, xm))
+        got = sorted([p["E_rev"], p["E_fwd"]])
+        assert max(abs(a - b_) for a, b_ in zip(got, sorted(ref))) < E_TOL
+        assert p["barrier"] == p["E_sp"] - p["E_rev"]
+
+
 def test_minimise_matches_oracle(gpu, oracle, odata, geam, search_mod, clusters):
     S, O = search_mod, oracle
     lopt = S.LBFGSOptions.defaults(f2norm=1e-4)
