@@ -109,6 +109,24 @@ class Clocks:
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def reduce_max(x: float, device=None) -> float:
+    """Maximum of x over the ranks of the default process group (x itself without one)."""
+    import torch
+    import torch.distributed as tdist
+
+    if not (tdist.is_available() and tdist.is_initialized()):
+        return float(x)
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(units_per_rank: int, world: int, steps: int, max_ms: float) -> float:
+    """Whole-job throughput of `world` independent replicas: every rank's units over the slowest rank's
+    time (weak scaling, no data-path collective)."""
+    return units_per_rank * world * steps / (max_ms * 1e-3)
+
+
 def measured_peak_hbm() -> tuple[float, str]:
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -359,12 +377,8 @@ def ours(args):
     ktimes = nl.kernel_times()
     clk = clocks.stop()
     nl.sync()
-    ms = ev0.elapsed_time(ev1)
-    if dist:
-        t = torch.tensor([ms], device=dev)
-        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = n * world * args.steps / (ms * 1e-3)
+    ms = reduce_max(ev0.elapsed_time(ev1), dev)
+    value = replica_value(n, world, args.steps, ms)
 
     # e2e through the host C ABI with pinned host buffers
     h_fields = [torch.from_numpy(f.reshape(-1)).pin_memory() for f in fields]
@@ -390,11 +404,7 @@ def ours(args):
     t0 = time.perf_counter()
     for j, sign, rb in sched:
         step_host(j, sign, rb)
-    e2e_s = time.perf_counter() - t0
-    if dist:
-        t = torch.tensor([e2e_s], device=dev)
-        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = reduce_max(time.perf_counter() - t0, dev)
     n_rb = sum(1 for _, _, rb in sched if rb)
     h2d = 24 * n  # a displacement field, or the positions on rebuild steps
     d2h = 24 * n + 8
