@@ -180,9 +180,10 @@ typedef struct {
 } flygpu_search_result;
 
 /* Launch shape of the batched search kernel: lanes per atom in the EAM passes (1, 2, 4, 8),
- * threads per CTA (multiple of 32) and resident CTAs per SM of the persistent grid. */
+ * threads per CTA (multiple of 32), resident CTAs per SM of the persistent grid and the kernel
+ * variant's register cap (0 = the compiler's allocation, 128 = at most 128 registers a thread). */
 typedef struct {
-  int lanes_per_atom, threads, blocks_per_sm, pad_;
+  int lanes_per_atom, threads, blocks_per_sm, max_registers;
 } flygpu_tuning;
 
 typedef struct flygpu_batch flygpu_batch;

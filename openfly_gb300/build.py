@@ -58,7 +58,7 @@ def build(verbose: bool = False) -> str:
     os.makedirs(OUT_DIR, exist_ok=True)
     nvcc = _nvcc()
     srcs = sources()
-    with ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
+    with ThreadPoolExecutor(max_workers=max(1, min(len(srcs), os.cpu_count() or 8))) as ex:
         objs = list(ex.map(lambda s: _compile(nvcc, s, verbose), srcs))
     if not os.path.exists(LIB) or os.path.getmtime(LIB) < max(os.path.getmtime(o) for o in objs):
         cmd = [nvcc, *ARCH, "-shared", "-o", LIB + ".tmp", *objs, "-lcudart"]

@@ -70,6 +70,7 @@ namespace flygpu {
     std::uint16_t* need;    // atoms whose F' the force pass reads (mobile atoms and their neighbours)
     std::uint16_t* mnbr;    // [NB_CAP][n]: mobile neighbours of each needed static atom
     std::uint16_t* mcnt;    // per atom: count in mnbr
+    long long* dacc;        // per atom: its mobile neighbours' density terms in fixed point (L2 atomics)
     int n_need, pad2;
     double trust, acc, convex, curv, energy;
     std::int64_t grad_calls;
@@ -90,12 +91,29 @@ namespace flygpu {
 
   // Byte offsets of one search's arrays inside its block (256-byte aligned parts).
   struct SearchLayout {
-    std::size_t xl, pk, type, aatom, ncnt, nbr, vec, hist, mob, rho0, need, mnbr, mcnt, total;
+    std::size_t xl, pk, type, aatom, ncnt, nbr, vec, hist, mob, rho0, need, mnbr, mcnt, dacc, total;
   };
 
+  // search_{m,d}{1,2,4,8}.cu: the kernel variants of one precision and lanes-per-atom.
+  using SearchKernel = void (*)(BatchView);
+  struct SearchKernels {
+    SearchKernel k[2];  // [0] the compiler's register allocation, [1] at most 128 registers a thread
+  };
+  template <bool MIXED, int LPA>
+  SearchKernels search_kernels();
+  template <> SearchKernels search_kernels<true, 1>();
+  template <> SearchKernels search_kernels<true, 2>();
+  template <> SearchKernels search_kernels<true, 4>();
+  template <> SearchKernels search_kernels<true, 8>();
+  template <> SearchKernels search_kernels<false, 1>();
+  template <> SearchKernels search_kernels<false, 2>();
+  template <> SearchKernels search_kernels<false, 4>();
+  template <> SearchKernels search_kernels<false, 8>();
+
   // search.cu
-  void search_launch(BatchView const& v, int lanes_per_atom, int threads, int blocks, bool mixed, cudaStream_t s);
-  void search_occupancy(int lanes_per_atom, int threads, bool mixed, int* blocks_per_sm);
+  void search_launch(BatchView const& v, int lanes_per_atom, int threads, int max_registers, int blocks, bool mixed,
+                     cudaStream_t s);
+  void search_occupancy(int lanes_per_atom, int threads, bool mixed, int max_registers, int* blocks_per_sm);
   SearchLayout search_layout(int n, int na, int n_vec_doubles, int n_hist_doubles);
   void search_bind(SearchDev& S, char* base, SearchLayout const& l);
 

@@ -1,0 +1,4 @@
+// Batched search kernels: binary64, 2 lanes per atom (both register variants).
+#include "search_kernel.cuh"
+
+FLYGPU_SEARCH_KERNELS(false, 2)

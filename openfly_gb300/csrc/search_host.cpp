@@ -161,14 +161,15 @@ namespace flygpu {
       std::ifstream in(p);
       std::string key;
       flygpu_tuning t{};
-      while (in >> key >> t.lanes_per_atom >> t.threads >> t.blocks_per_sm) g_tune_cache[key] = t;
+      while (in >> key >> t.lanes_per_atom >> t.threads >> t.blocks_per_sm >> t.max_registers) g_tune_cache[key] = t;
     }
 
     void save_file_cache() {
       std::string const p = cache_path();
       if (p.empty()) return;
       std::ofstream out(p, std::ios::trunc);
-      for (auto const& [k, t] : g_tune_cache) out << k << ' ' << t.lanes_per_atom << ' ' << t.threads << ' ' << t.blocks_per_sm << '\n';
+      for (auto const& [k, t] : g_tune_cache)
+        out << k << ' ' << t.lanes_per_atom << ' ' << t.threads << ' ' << t.blocks_per_sm << ' ' << t.max_registers << '\n';
     }
 
   }  // namespace
@@ -329,7 +330,8 @@ namespace flygpu {
     if (t.threads % 32 || t.threads < 32 || t.threads > 1024) fail(FLYGPU_INVALID_ARG, "bad threads per CTA");
     int const blocks = std::max(1, std::min(n_items, std::max(1, t.blocks_per_sm) * sm_count()));
     FLY_CUDA(cudaMemsetAsync(B->work.p, 0, sizeof(int), B->stream));
-    search_launch(B->view(ord, n_items, budget), t.lanes_per_atom, t.threads, blocks, B->mixed, B->stream);
+    search_launch(B->view(ord, n_items, budget), t.lanes_per_atom, t.threads, t.max_registers, blocks, B->mixed,
+                  B->stream);
   }
 
   flygpu_tuning autotune(flygpu_batch* B) {
@@ -353,21 +355,23 @@ namespace flygpu {
     float best_ms = 1e30f;
     for (int lpa : {1, 2, 4, 8}) {
       for (int threads : {128, 256}) {
-        flygpu_tuning t{lpa, threads, 0, 0};
-        int bps = 0;
-        // resident CTAs per SM for this shape
-        search_occupancy(lpa, threads, B->mixed, &bps);
-        t.blocks_per_sm = std::max(1, bps);
-        batch_reset(B);
-        FLY_CUDA(cudaEventRecord(e0, B->stream));
-        batch_launch(B, t, ord.p, want, 0);
-        FLY_CUDA(cudaEventRecord(e1, B->stream));
-        FLY_CUDA(cudaEventSynchronize(e1));
-        float ms = 0;
-        FLY_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-        if (ms < best_ms) {
-          best_ms = ms;
-          best = t;
+        for (int regs : {0, 128}) {
+          flygpu_tuning t{lpa, threads, 0, regs};
+          int bps = 0;
+          // resident CTAs per SM for this shape
+          search_occupancy(lpa, threads, B->mixed, regs, &bps);
+          t.blocks_per_sm = std::max(1, bps);
+          batch_reset(B);
+          FLY_CUDA(cudaEventRecord(e0, B->stream));
+          batch_launch(B, t, ord.p, want, 0);
+          FLY_CUDA(cudaEventRecord(e1, B->stream));
+          FLY_CUDA(cudaEventSynchronize(e1));
+          float ms = 0;
+          FLY_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+          if (ms < best_ms) {
+            best_ms = ms;
+            best = t;
+          }
         }
       }
     }

@@ -1,0 +1,4 @@
+// Batched search kernels: binary32 pairs / binary64 accumulation, 8 lanes per atom (both register variants).
+#include "search_kernel.cuh"
+
+FLYGPU_SEARCH_KERNELS(true, 8)

@@ -142,7 +142,7 @@ void flygpu_server::tick_graph() {
     return n;
   }();
   int const blocks = std::max(1, std::min(max_active, std::max(1, tuning.blocks_per_sm) * sms));
-  search_launch(v, tuning.lanes_per_atom, tuning.threads, blocks, mixed, compute);
+  search_launch(v, tuning.lanes_per_atom, tuning.threads, tuning.max_registers, blocks, mixed, compute);
   FLY_CUDA(cudaMemcpyAsync(h_S.p, S.p, sizeof(SearchDev) * static_cast<std::size_t>(max_active), cudaMemcpyDeviceToHost,
                            compute));
   FLY_CUDA(cudaStreamEndCapture(compute, &g));

@@ -76,10 +76,12 @@ class SearchResult(C.Structure):
 
 
 class Tuning(C.Structure):
-    _fields_ = [("lanes_per_atom", C.c_int), ("threads", C.c_int), ("blocks_per_sm", C.c_int), ("pad_", C.c_int)]
+    _fields_ = [("lanes_per_atom", C.c_int), ("threads", C.c_int), ("blocks_per_sm", C.c_int),
+                ("max_registers", C.c_int)]
 
     def as_dict(self) -> dict:
-        return {"lanes_per_atom": self.lanes_per_atom, "threads": self.threads, "blocks_per_sm": self.blocks_per_sm}
+        return {"lanes_per_atom": self.lanes_per_atom, "threads": self.threads, "blocks_per_sm": self.blocks_per_sm,
+                "max_registers": self.max_registers}
 
 
 _ready = False

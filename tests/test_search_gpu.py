@@ -100,6 +100,23 @@ def test_same_alone_and_in_mix(gpu, geam, search_mod, clusters):
         assert np.array_equal(p[0], pos_mix[k])
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_register_capped_variant_is_the_same_search(gpu, geam, search_mod, clusters, precision):
+    # The 128-register kernel differs from the default one only in register allocation.
+    S = search_mod
+    prec = gpu.FP64 if precision == "fp64" else gpu.MIXED
+    b = S.Batch(geam, [S.from_cluster(c) for c in clusters[:12]], precision=prec,
+                dimer=S.DimerOptions.defaults(n=6, rot_n=6, f2norm=1e-3))
+    out = []
+    for regs in (0, 128):
+        b.reset()
+        b.run(S.Tuning(2, 128, 4, regs))
+        out.append(b.results())
+    (r0, p0, _), (r1, p1, _) = out
+    assert r0 == r1
+    assert all(np.array_equal(a, c) for a, c in zip(p0, p1))
+
+
 def test_batch_rerun_after_reset_is_identical(gpu, geam, search_mod, clusters):
     S = search_mod
     b = S.Batch(geam, [S.from_cluster(c) for c in clusters[:6]], precision=gpu.MIXED,
