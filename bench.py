@@ -339,7 +339,10 @@ def ours(args):
     if dist:
         tdist.barrier()
     dev = torch.device("cuda", local)
-    stream = torch.cuda.current_stream(dev)
+    # A stream of our own: the list launches every kernel on it and the timing events are recorded on it
+    # (handle 0 would make the library create a private non-blocking stream the events do not see).
+    stream = torch.cuda.Stream(device=dev)
+    torch.cuda.set_stream(stream)
 
     s, fields = make_workload(args.cells)
     n = s.n
@@ -456,6 +459,28 @@ def ours(args):
         tdist.destroy_process_group()
 
 
+def search_batch(args) -> None:
+    """One batched launch over --search-batch config-3 clusters (lanes 2, 128 threads, 2 CTAs/SM), for
+    profiling the search kernel on a small case; prints one JSON line (not a bench line)."""
+    import openfly_gb300 as fly
+    from openfly_gb300 import search as S
+    from openfly_gb300 import workloads as W
+    from openfly_gb300.build import build
+
+    build()
+    eam = fly.EAM(W.TABLE)
+    opt = S.DimerOptions.defaults(n=6, rot_n=6, f2norm=1e-3, max_steps=args.max_search_steps)
+    prec = fly.MIXED if args.precision == "mixed" else fly.FP64
+    b = S.Batch(eam, [S.from_cluster(c) for c in W.config3(n=args.search_batch, seed=7)], precision=prec, dimer=opt)
+    t0 = time.perf_counter()
+    b.run(S.Tuning(2, 128, 2, 0))
+    res, _, _ = b.results(positions=False)
+    dt = time.perf_counter() - t0
+    print(json.dumps({"search_batch": len(res), "precision": args.precision, "seconds": dt,
+                      "grad_calls": int(sum(r["grad_calls"] for r in res)),
+                      "errors": int(sum(r["status"] != 0 for r in res))}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--gpus", type=int, default=1)
@@ -470,10 +495,16 @@ def main():
     ap.add_argument("--plain-sample", type=int, default=32, help="searches timed on the plain path")
     ap.add_argument("--arrival-rate", type=float, default=3000.0, help="served requests per second (Poisson)")
     ap.add_argument("--steps-per-tick", type=int, default=8, help="translation steps per serving tick")
+    ap.add_argument("--search-batch", type=int, default=0,
+                    help="only run one batch of this many config-3 searches (a small case for profilers)")
+    ap.add_argument("--max-search-steps", type=int, default=1000, help="translation-step limit of --search-batch")
+    ap.add_argument("--precision", choices=["mixed", "fp64"], default="mixed", help="precision of --search-batch")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")
-    if args.impl == "reference":
+    if args.search_batch > 0:
+        search_batch(args)
+    elif args.impl == "reference":
         reference_arm(args)
     else:
         ours(args)

@@ -2,6 +2,8 @@
 // output gather and the choice among the kernel variants (search_kernel.cuh; one translation unit per
 // precision and lanes-per-atom, search_{m,d}{1,2,4,8}.cu).
 
+#include <mutex>
+
 #include "search.hpp"
 
 namespace flygpu {
@@ -99,16 +101,30 @@ namespace flygpu {
     launch(k_gather_out, v.n_search, 128, 0, s, v, d_act3_off, out_x, out_ax);
   }
 
-  void search_occupancy(int lanes_per_atom, int threads, bool mixed, int max_registers, int* blocks_per_sm) {
+  void search_init_kernels() {
+    static std::once_flag once;
+    std::call_once(once, [] {
+      for (bool mixed : {true, false})
+        for (int lpa : {1, 2, 4, 8})
+          for (SearchKernel k : kernels(mixed, lpa).k)
+            FLY_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, SEARCH_SMEM_CAP));
+    });
+  }
+
+  void search_occupancy(int lanes_per_atom, int threads, bool mixed, int max_registers, int smem_bytes,
+                        int* blocks_per_sm) {
+    search_init_kernels();
     FLY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, pick(mixed, lanes_per_atom, max_registers),
-                                                           threads, 0));
+                                                           threads, static_cast<std::size_t>(smem_bytes)));
   }
 
   void search_launch(BatchView const& v, int lanes_per_atom, int threads, int max_registers, int blocks, bool mixed,
                      cudaStream_t s) {
     if (threads % 32 != 0 || threads < 64 || threads > 1024)
       fail(FLYGPU_INVALID_ARG, "threads must be 64..1024, a multiple of 32");
-    launch(pick(mixed, lanes_per_atom, max_registers), blocks, threads, 0, s, v);
+    if (v.smem_bytes < 0 || v.smem_bytes > SEARCH_SMEM_CAP) fail(FLYGPU_INVALID_ARG, "search shared memory out of range");
+    search_init_kernels();
+    launch(pick(mixed, lanes_per_atom, max_registers), blocks, threads, static_cast<std::size_t>(v.smem_bytes), s, v);
   }
 
 }  // namespace flygpu

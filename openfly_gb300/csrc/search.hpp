@@ -12,6 +12,16 @@ namespace flygpu {
   constexpr int MAX_ATOMS = 4096;  // atoms per search (local indices fit in uint16 with room to spare)
   constexpr int MAX_HIST = 16;     // L-BFGS history length supported on the device
   constexpr int N_VEC = 15;        // fixed per-DOF vectors of a search (see Vec below)
+  // Dynamic shared memory a CTA may use to stage the search it runs (vectors, positions, slot records):
+  // two CTAs of this size fit in one SM's 228 KB.
+  constexpr int SEARCH_SMEM_CAP = 100 * 1024;
+
+  // Bytes of the shared-memory image of a search of n atoms whose vectors hold n_vec_doubles doubles:
+  // vectors (rounded to 128 B), then positions (D4), then binary32 slot records.
+  inline std::size_t search_smem_need(int n, std::size_t n_vec_doubles) {
+    std::size_t const vb = (n_vec_doubles * sizeof(double) + 127) / 128 * 128;
+    return vb + static_cast<std::size_t>(n) * (sizeof(D4) + sizeof(Packed));
+  }
 
   enum Mode : int { MODE_DIMER = 0, MODE_MINIMISE = 1 };
   enum Stage : int { STAGE_INIT = 0, STAGE_LOOP = 1, STAGE_DONE = 2 };
@@ -85,6 +95,7 @@ namespace flygpu {
     int const* n_items_dev;   // if set, the item count is read from device memory (graph replays)
     int* work;                // atomic work counter
     int budget;               // translation steps per launch (<= 0: run to completion)
+    int smem_bytes;           // dynamic shared memory per CTA for staging a search's state (0: none)
     SearchOpts o;
     TablesView tb;
   };
@@ -113,7 +124,11 @@ namespace flygpu {
   // search.cu
   void search_launch(BatchView const& v, int lanes_per_atom, int threads, int max_registers, int blocks, bool mixed,
                      cudaStream_t s);
-  void search_occupancy(int lanes_per_atom, int threads, bool mixed, int max_registers, int* blocks_per_sm);
+  void search_occupancy(int lanes_per_atom, int threads, bool mixed, int max_registers, int smem_bytes,
+                        int* blocks_per_sm);
+  // Lets every kernel variant use SEARCH_SMEM_CAP bytes of dynamic shared memory (once per process;
+  // call before any graph capture).
+  void search_init_kernels();
   SearchLayout search_layout(int n, int na, int n_vec_doubles, int n_hist_doubles);
   void search_bind(SearchDev& S, char* base, SearchLayout const& l);
 

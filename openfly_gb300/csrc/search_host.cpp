@@ -90,6 +90,7 @@ struct flygpu_batch {
   std::int64_t bytes = 0;
   std::int64_t total_atoms = 0, total_act = 0;
   std::size_t block_bytes = 0;
+  int smem_bytes = 0;  // dynamic shared memory per CTA for staging searches (search_smem_need, capped)
   bool tuned = false;
   flygpu_tuning tuning{};
   std::string tune_key;
@@ -102,6 +103,7 @@ struct flygpu_batch {
     v.n_items = n_items;
     v.work = work.p;
     v.budget = budget;
+    v.smem_bytes = smem_bytes;
     v.o = o;
     v.tb = eam->view();
     return v;
@@ -283,7 +285,12 @@ namespace flygpu {
       B->h_aatom.insert(B->h_aatom.end(), mob.begin(), mob.end());
       atoms += n;
       act += na;
+      bool const dimer = d.mode == FLYGPU_SEARCH_DIMER;
+      int const mT = dimer ? B->o.mT : B->o.mL, mR = dimer ? B->o.mR : 0;
+      std::size_t const need = search_smem_need(n, static_cast<std::size_t>(N_VEC + 2 * mT + 2 * mR) * 3 * na);
+      B->smem_bytes = static_cast<int>(std::min<std::size_t>(SEARCH_SMEM_CAP, std::max<std::size_t>(B->smem_bytes, need)));
     }
+    search_init_kernels();
     B->total_atoms = atoms;
     B->total_act = act;
     B->block_bytes = off;
@@ -359,7 +366,7 @@ namespace flygpu {
           flygpu_tuning t{lpa, threads, 0, regs};
           int bps = 0;
           // resident CTAs per SM for this shape
-          search_occupancy(lpa, threads, B->mixed, regs, &bps);
+          search_occupancy(lpa, threads, B->mixed, regs, B->smem_bytes, &bps);
           t.blocks_per_sm = std::max(1, bps);
           batch_reset(B);
           FLY_CUDA(cudaEventRecord(e0, B->stream));

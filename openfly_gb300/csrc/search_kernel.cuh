@@ -47,6 +47,7 @@ namespace flygpu {
     struct Blk {
       double red[32];
       double rhoR[MAX_HIST], alphaR[MAX_HIST];
+      double rhoT[MAX_HIST], alphaT[MAX_HIST];  // the translation L-BFGS scalars, staged from SearchDev
       double curv;
       int n_need;  // atoms in the current needed list
       int item;
@@ -1262,42 +1263,76 @@ namespace flygpu {
     // ------------------------------------------------------------------ one search
 
     template <bool MIXED, int LPA>
-    __device__ void run(BatchView const& bv, Blk& sh, int sidx) {
+    __device__ void run(BatchView const& bv, Blk& sh, Ctx& cs, int sidx) {
       SearchDev* S = bv.S + sidx;
       if (S->stage == STAGE_DONE) return;
       SearchOpts const& o = bv.o;
-      Ctx c;
-      c.S = S;
-      c.n = S->n;
-      c.na = S->na;
-      c.M = 3 * S->na;
+      Ctx cl;  // this thread's copy while it is set up; the block then reads the shared one (cs)
+      cl.S = S;
+      cl.n = S->n;
+      cl.na = S->na;
+      cl.M = 3 * S->na;
       bool const dimer = S->mode == MODE_DIMER;
-      c.mT = dimer ? o.mT : o.mL;
-      c.mR = dimer ? o.mR : 0;
-      c.xl = S->xl;
-      c.pk = S->pk;
-      c.ty = S->type;
-      c.aatom = S->aatom;
-      c.ncnt = S->ncnt;
-      c.nbr = S->nbr;
-      c.v = S->vec;
-      c.hist = S->hist;
-      c.mob = S->mob;
-      c.rho0 = S->rho0;
-      c.need = S->need;
-      c.mnbr = S->mnbr;
-      c.mcnt = S->mcnt;
-      c.dacc = S->dacc;
-      c.rc2 = o.r_cut * o.r_cut;
-      c.rc2f = static_cast<float>(c.rc2);
-      c.periodic = S->periodic_any != 0;
+      cl.mT = dimer ? o.mT : o.mL;
+      cl.mR = dimer ? o.mR : 0;
+      cl.xl = S->xl;
+      cl.pk = S->pk;
+      cl.ty = S->type;
+      cl.aatom = S->aatom;
+      cl.ncnt = S->ncnt;
+      cl.nbr = S->nbr;
+      cl.v = S->vec;
+      cl.hist = S->hist;
+      cl.mob = S->mob;
+      cl.rho0 = S->rho0;
+      cl.need = S->need;
+      cl.mnbr = S->mnbr;
+      cl.mcnt = S->mcnt;
+      cl.dacc = S->dacc;
+      cl.rc2 = o.r_cut * o.r_cut;
+      cl.rc2f = static_cast<float>(cl.rc2);
+      cl.periodic = S->periodic_any != 0;
       for (int k = 0; k < 3; ++k) {
-        c.L[k] = S->L[k];
-        c.invL[k] = 1.0 / S->L[k];
-        c.Lf[k] = static_cast<float>(S->L[k]);
-        c.per[k] = S->per[k] != 0;
-        c.shift[k] = S->shift[k];
+        cl.L[k] = S->L[k];
+        cl.invL[k] = 1.0 / S->L[k];
+        cl.Lf[k] = static_cast<float>(S->L[k]);
+        cl.per[k] = S->per[k] != 0;
+        cl.shift[k] = S->shift[k];
       }
+      // Stage the search's vectors, positions and binary32 slot records in this CTA's dynamic shared
+      // memory for the launch, as far as they fit (in that order). All three are rewritten every step,
+      // so from global memory each dependent step would be an L2 round trip.
+      extern __shared__ __align__(128) unsigned char dsm[];
+      std::size_t const vb = static_cast<std::size_t>(N_VEC + 2 * cl.mT + 2 * cl.mR) * static_cast<std::size_t>(cl.M);
+      std::size_t const vbr = (vb * sizeof(double) + 127) / 128 * 128;
+      std::size_t const xb = static_cast<std::size_t>(cl.n) * sizeof(D4);
+      std::size_t const pb = static_cast<std::size_t>(cl.n) * sizeof(Packed);
+      std::size_t const cap = static_cast<std::size_t>(bv.smem_bytes);
+      bool const st_v = vbr <= cap, st_x = vbr + xb <= cap, st_p = vbr + xb + pb <= cap;
+      if (st_v) {
+        double* v = reinterpret_cast<double*>(dsm);
+        for (std::size_t e = threadIdx.x; e < vb; e += blockDim.x) v[e] = S->vec[e];
+        cl.v = v;
+      }
+      if (st_x) {
+        double2* x = reinterpret_cast<double2*>(dsm + vbr);
+        double2 const* g = reinterpret_cast<double2 const*>(S->xl);
+        for (std::size_t e = threadIdx.x; e < xb / 16; e += blockDim.x) x[e] = g[e];
+        cl.xl = reinterpret_cast<D4*>(x);
+      }
+      if (st_p) {
+        float4* q = reinterpret_cast<float4*>(dsm + vbr + xb);
+        float4 const* g = reinterpret_cast<float4 const*>(S->pk);
+        for (std::size_t e = threadIdx.x; e < pb / 16; e += blockDim.x) q[e] = g[e];
+        cl.pk = reinterpret_cast<Packed*>(q);
+      }
+      for (int h = threadIdx.x; h < MAX_HIST; h += blockDim.x) {
+        sh.rhoT[h] = S->rhoT[h];
+        sh.alphaT[h] = S->alphaT[h];
+      }
+      if (threadIdx.x == 0) cs = cl;
+      __syncthreads();
+      Ctx const& c = cs;
       TablesView const& tb = bv.tb;
       double const skin = S->rc_list - (dimer ? o.r_cut + 2 * o.delta_r : o.r_cut);
       double* X = c.V(V_X);
@@ -1398,7 +1433,7 @@ namespace flygpu {
             }
           }
           if (act == ACT_GO) {
-            newton<MIXED>(c, c.mT, kT, c.sT(0), c.yT(0), S->rhoT, S->alphaT, c.V(V_PXT), c.V(V_PGT), X, eff, hg);
+            newton<MIXED>(c, c.mT, kT, c.sT(0), c.yT(0), sh.rhoT, sh.alphaT, c.V(V_PXT), c.V(V_PGT), X, eff, hg);
             double const nrm = wdot<MIXED>(hg, hg, M);
             double const tr = trust;
             double const sc = scal<MIXED>([&] { return fminf(1.f, static_cast<float>(tr) * rsqrtf(static_cast<float>(nrm))); },
@@ -1467,6 +1502,23 @@ namespace flygpu {
         }
       }
       __syncthreads();
+      if (st_v) {
+        for (std::size_t e = threadIdx.x; e < vb; e += blockDim.x) S->vec[e] = c.v[e];
+      }
+      if (st_x) {
+        double2 const* x = reinterpret_cast<double2 const*>(c.xl);
+        double2* g = reinterpret_cast<double2*>(S->xl);
+        for (std::size_t e = threadIdx.x; e < xb / 16; e += blockDim.x) g[e] = x[e];
+      }
+      if (st_p) {
+        float4 const* q = reinterpret_cast<float4 const*>(c.pk);
+        float4* g = reinterpret_cast<float4*>(S->pk);
+        for (std::size_t e = threadIdx.x; e < pb / 16; e += blockDim.x) g[e] = q[e];
+      }
+      for (int h = threadIdx.x; h < MAX_HIST; h += blockDim.x) {
+        S->rhoT[h] = sh.rhoT[h];
+        S->alphaT[h] = sh.alphaT[h];
+      }
       if (threadIdx.x == 0) {
         S->kT = kT;
         S->n_need = sh.n_need;
@@ -1490,6 +1542,7 @@ namespace flygpu {
     template <bool MIXED, int LPA>
     __device__ __forceinline__ void search_items(BatchView const& bv) {
       __shared__ Blk sh;
+      __shared__ Ctx cs;
       int const n_items = bv.n_items_dev ? *bv.n_items_dev : bv.n_items;
       for (;;) {
         if (threadIdx.x == 0) sh.item = atomicAdd(bv.work, 1);
@@ -1497,7 +1550,7 @@ namespace flygpu {
         int const item = sh.item;
         __syncthreads();
         if (item >= n_items) break;
-        run<MIXED, LPA>(bv, sh, bv.order[item]);
+        run<MIXED, LPA>(bv, sh, cs, bv.order[item]);
       }
     }
 

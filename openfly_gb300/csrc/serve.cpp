@@ -133,6 +133,7 @@ void flygpu_server::tick_graph() {
   v.n_items_dev = order.p;
   v.work = work.p;
   v.budget = steps_per_tick;
+  v.smem_bytes = SEARCH_SMEM_CAP;
   v.o = o;
   v.tb = eam->view();
   int const sms = [] {
@@ -333,6 +334,7 @@ int flygpu_server_create(flygpu_eam* eam, const flygpu_dimer_options* dimer, con
     std::memcpy(srv->h_S.p, idle.data(), sizeof(SearchDev) * idle.size());
     FLY_CUDA(cudaMemcpy(srv->S.p, idle.data(), sizeof(SearchDev) * idle.size(), cudaMemcpyHostToDevice));
     srv->slots.resize(static_cast<std::size_t>(max_active));
+    search_init_kernels();  // before the capture
     srv->tick_graph();
     srv->worker = std::thread([p = srv.get()] { p->loop(); });
     *out = srv.release();
