@@ -425,7 +425,7 @@ namespace flygpu {
 
     // Force pass over mobile atoms into out (3 per mobile atom).
     template <bool MIXED, int LPA>
-    __device__ void force(Ctx const& c, TablesView const& tb, Blk& sh, double* out) {
+    __device__ void force(Ctx const& c, TablesView const& tb, Blk& sh, typename std::conditional<MIXED, float, double>::type* out) {
       int const nt = blockDim.x;
       int const total = c.na * LPA;
       int const rounds = (total + nt - 1) / nt;
@@ -492,9 +492,10 @@ namespace flygpu {
         gy = lane_sum<LPA>(gy);
         gz = lane_sum<LPA>(gz);
         if (valid && l == 0) {
-          out[3 * k0 + 0] = gx;
-          out[3 * k0 + 1] = gy;
-          out[3 * k0 + 2] = gz;
+          using O = typename std::conditional<MIXED, float, double>::type;
+          out[3 * k0 + 0] = static_cast<O>(gx);
+          out[3 * k0 + 1] = static_cast<O>(gy);
+          out[3 * k0 + 2] = static_cast<O>(gz);
         }
       }
     }
@@ -807,7 +808,7 @@ namespace flygpu {
     }
 
     template <bool MIXED, int W>
-    __device__ void passes(Ctx const& c, TablesView const& tb, Blk& sh, double* out) {
+    __device__ void passes(Ctx const& c, TablesView const& tb, Blk& sh, typename std::conditional<MIXED, float, double>::type* out) {
       density_inc<MIXED, W>(c, tb, sh);
       __syncthreads();
       force<MIXED, W>(c, tb, sh, out);
@@ -816,7 +817,7 @@ namespace flygpu {
     // One EAM gradient evaluation into out (mobile DOFs). Called by every thread; returns true when a
     // device-side error was raised (the caller ends the search).
     template <bool MIXED, int LPA>
-    __device__ bool gradient(Ctx const& c, TablesView const& tb, Blk& sh, double* out) {
+    __device__ bool gradient(Ctx const& c, TablesView const& tb, Blk& sh, typename std::conditional<MIXED, float, double>::type* out) {
       __syncthreads();
       if (MIXED) {
         for (int k = threadIdx.x; k < c.na; k += blockDim.x) pack_one(c, c.aatom[k]);
@@ -980,14 +981,25 @@ namespace flygpu {
     template <bool MIXED>
     using Red = typename std::conditional<MIXED, float, double>::type;
 
+    // Storage of a search's per-DOF vectors other than positions: binary32 in binary32-pair searches
+    // (a vector keeps its M-double slot and uses the first half of it), binary64 otherwise. Positions
+    // (V_X, V_INMIN, the translation L-BFGS's previous x) are binary64 in both.
     template <bool MIXED>
-    __device__ inline double wsum(Red<MIXED> v) {
-      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
-      return static_cast<double>(v);
+    using Vt = typename std::conditional<MIXED, float, double>::type;
+
+    template <bool MIXED>
+    __device__ inline Vt<MIXED>* vp(double* slot) {
+      return reinterpret_cast<Vt<MIXED>*>(slot);
     }
 
     template <bool MIXED>
-    __device__ inline double wdot(double const* a, double const* b, int M) {
+    __device__ inline Red<MIXED> wsum(Red<MIXED> v) {
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
+      return v;
+    }
+
+    template <bool MIXED, typename A, typename B>
+    __device__ inline Red<MIXED> wdot(A const* a, B const* b, int M) {
       Red<MIXED> s = 0;
       for (int e = threadIdx.x; e < M; e += 32) s += static_cast<Red<MIXED>>(a[e]) * static_cast<Red<MIXED>>(b[e]);
       return wsum<MIXED>(s);
@@ -1005,30 +1017,34 @@ namespace flygpu {
     }
 
     // List::update (list.cpp:37-51) on mobile atoms: xl -= d (warp 0).
-    __device__ inline void wlist_update(Ctx const& c, double const* d, double sign) {
-      for (int e = threadIdx.x; e < c.M; e += 32) comp(c.xl[c.aatom[e / 3]], e % 3) -= sign * d[e];
+    template <typename T>
+    __device__ inline void wlist_update(Ctx const& c, T const* d, double sign) {
+      for (int e = threadIdx.x; e < c.M; e += 32) comp(c.xl[c.aatom[e / 3]], e % 3) -= sign * static_cast<double>(d[e]);
     }
 
-    // StepLBFGS::newton_step_impl (lbfgs_core.cpp:29-87), warp 0. s(j) = s0 + j M, y(j) = y0 + j M.
-    template <bool MIXED>
+    // StepLBFGS::newton_step_impl (lbfgs_core.cpp:29-87), warp 0. History slot j of s (y) starts at
+    // s0 + j M (y0 + j M) doubles and holds a V vector. x / px are positions (binary64) for the
+    // translation and the axis (V) for the rotation.
+    template <bool MIXED, typename XT>
     __device__ void newton(Ctx const& c, int m, int& k, double* s0, double* y0, double* rho, double* alpha,
-                           double* px, double* pg, double const* x, double const* g, double* out) {
+                           XT* px, Vt<MIXED>* pg, XT const* x, Vt<MIXED> const* g, Vt<MIXED>* out) {
       using R = Red<MIXED>;
+      using V = Vt<MIXED>;
       int const M = c.M;
       int const lane = threadIdx.x;
-      auto S_ = [&](int j) { return s0 + static_cast<std::int64_t>(j) * M; };
-      auto Y_ = [&](int j) { return y0 + static_cast<std::int64_t>(j) * M; };
+      auto S_ = [&](int j) { return vp<MIXED>(s0 + static_cast<std::int64_t>(j) * M); };
+      auto Y_ = [&](int j) { return vp<MIXED>(y0 + static_cast<std::int64_t>(j) * M); };
       int const prev = k > 0 ? (k - 1) % m : 0;
       if (k > 0) {
-        double* sp = S_(prev);
-        double* yp = Y_(prev);
+        V* sp = S_(prev);
+        V* yp = Y_(prev);
         R d = 0;
         for (int e = lane; e < M; e += 32) {
-          sp[e] = x[e] - px[e];
+          sp[e] = static_cast<V>(x[e] - px[e]);
           yp[e] = g[e] - pg[e];
           d += static_cast<R>(sp[e]) * static_cast<R>(yp[e]);
         }
-        double const ds = wsum<MIXED>(d);
+        R const ds = wsum<MIXED>(d);
         double const r = scal<MIXED>([&] { return 1.f / fabsf(static_cast<float>(ds)); },
                                      [&] { return 1.0 / fabs(ds); });
         if (lane == 0) rho[prev] = r;
@@ -1043,41 +1059,43 @@ namespace flygpu {
       int const bound = k <= m ? k : m;
       for (int i = bound - 1; i >= 0; --i) {
         int const j = (i + incur) % m;
-        double const* s = S_(j);
-        double const* y = Y_(j);
-        double const a = rho[j] * wdot<MIXED>(s, out, M);
+        V const* s = S_(j);
+        V const* y = Y_(j);
+        R const a = static_cast<R>(rho[j]) * wdot<MIXED>(s, out, M);
         if (lane == 0) alpha[j] = a;
-        for (int e = lane; e < M; e += 32) out[e] -= a * y[e];
+        V const av = static_cast<V>(a);
+        for (int e = lane; e < M; e += 32) out[e] -= av * y[e];
       }
       if (k > 0) {
-        double const* yp = Y_(prev);
-        double const yy = wdot<MIXED>(yp, yp, M);
-        double const rp = rho[prev];
-        double const scale = scal<MIXED>([&] { return 1.f / static_cast<float>(rp) / static_cast<float>(yy); },
-                                         [&] { return 1.0 / rp / yy; });
+        V const* yp = Y_(prev);
+        R const yy = wdot<MIXED>(yp, yp, M);
+        R const rp = static_cast<R>(rho[prev]);
+        V const scale = static_cast<V>(scal<MIXED>([&] { return 1.f / static_cast<float>(rp) / static_cast<float>(yy); },
+                                                   [&] { return 1.0 / rp / yy; }));
         for (int e = lane; e < M; e += 32) out[e] = out[e] * scale;
       }
       __syncwarp();
       for (int i = 0; i <= bound - 1; ++i) {
         int const j = (i + incur) % m;
-        double const* s = S_(j);
-        double const* y = Y_(j);
-        double const beta = rho[j] * wdot<MIXED>(y, out, M);
-        double const a = alpha[j];
-        for (int e = lane; e < M; e += 32) out[e] += (a - beta) * s[e];
+        V const* s = S_(j);
+        V const* y = Y_(j);
+        R const beta = static_cast<R>(rho[j]) * wdot<MIXED>(y, out, M);
+        V const ab = static_cast<V>(static_cast<R>(alpha[j]) - beta);
+        for (int e = lane; e < M; e += 32) out[e] += ab * s[e];
       }
       __syncwarp();
       ++k;
     }
 
     // trans_proj (rotor.cpp:33-47), warp 0: remove the mean per component.
-    __device__ void trans_proj(Ctx const& c, double* x) {
+    template <typename T>
+    __device__ void trans_proj(Ctx const& c, T* x) {
       double p[3] = {0.0, 0.0, 0.0};
-      for (int e = threadIdx.x; e < c.M; e += 32) p[e % 3] += x[e];
+      for (int e = threadIdx.x; e < c.M; e += 32) p[e % 3] += static_cast<double>(x[e]);
       for (double& v : p) v = warp_sum(v);
       double const inv = lane0([&] { return 1.0 / static_cast<double>(c.na); });
       double const q[3] = {p[0] * inv, p[1] * inv, p[2] * inv};
-      for (int e = threadIdx.x; e < c.M; e += 32) x[e] -= q[e % 3];
+      for (int e = threadIdx.x; e < c.M; e += 32) x[e] = static_cast<T>(static_cast<double>(x[e]) - q[e % 3]);
       __syncwarp();
     }
 
@@ -1092,26 +1110,31 @@ namespace flygpu {
 
     // ------------------------------------------------------------------ Rotor::eff_gradient
 
-    // Returns true on a device-side error; the curvature lands in sh.curv.
+    // Returns true on a device-side error; the curvature lands in sh.curv. Vectors are V (binary32 in
+    // binary32-pair searches); every scalar is cast to V before it scales a vector, so the per-element
+    // work stays in V.
     template <bool MIXED, int LPA>
     __device__ bool eff_gradient(Ctx const& c, TablesView const& tb, SearchOpts const& o, Blk& sh) {
+      using V = Vt<MIXED>;
+      using R = Red<MIXED>;
       int const M = c.M;
       bool const lead = threadIdx.x < 32;
       int const lane = threadIdx.x & 31;
-      double* ax = c.V(V_AX);
-      double* g0 = c.V(V_G0);
-      double* g1 = c.V(V_G1);
-      double* g1p = c.V(V_G1P);
-      double* dprev = c.V(V_DPREV);
-      double* axp = c.V(V_AXP);
-      double* th = c.V(V_TH);
-      double* eff = c.V(V_EFF);
+      V* ax = vp<MIXED>(c.V(V_AX));
+      V* g0 = vp<MIXED>(c.V(V_G0));
+      V* g1 = vp<MIXED>(c.V(V_G1));
+      V* g1p = vp<MIXED>(c.V(V_G1P));
+      V* dprev = vp<MIXED>(c.V(V_DPREV));
+      V* axp = vp<MIXED>(c.V(V_AXP));
+      V* th = vp<MIXED>(c.V(V_TH));
+      V* eff = vp<MIXED>(c.V(V_EFF));
       double const dr = o.delta_r;
+      V const drv = static_cast<V>(dr);
       int kR = 0;
       double curv = 0;
       if (gradient<MIXED, LPA>(c, tb, sh, g0)) return true;
       if (lead) {
-        for (int e = lane; e < M; e += 32) dprev[e] = -dr * ax[e];
+        for (int e = lane; e < M; e += 32) dprev[e] = -drv * ax[e];
         __syncwarp();
         wlist_update(c, dprev, 1.0);
       }
@@ -1121,30 +1144,31 @@ namespace flygpu {
         double theta_1 = 0, b_1 = 0, c_x0 = 0;
         int act = ACT_GO;
         if (lead) {
-          using R = Red<MIXED>;
-          double* dg = g1p;  // scratch until the trial gradient is evaluated
+          V* dg = g1p;  // scratch until the trial gradient is evaluated
           R tl = 0;
           for (int e = lane; e < M; e += 32) {
             dg[e] = g1[e] - g0[e];
             tl += static_cast<R>(dg[e]) * static_cast<R>(ax[e]);
           }
-          double const t = wsum<MIXED>(tl);
+          V const t = static_cast<V>(wsum<MIXED>(tl));
           for (int e = lane; e < M; e += 32) dg[e] -= t * ax[e];
           __syncwarp();
           if (c.S->count_frozen == 0) trans_proj(c, dg);
-          newton<MIXED>(c, c.mR, kR, c.sR(0), c.yR(0), sh.rhoR, sh.alphaR, c.V(V_PXR), c.V(V_PGR), ax, dg, th);
-          double const tp = wdot<MIXED>(th, ax, M);
+          newton<MIXED>(c, c.mR, kR, c.sR(0), c.yR(0), sh.rhoR, sh.alphaR, vp<MIXED>(c.V(V_PXR)),
+                        vp<MIXED>(c.V(V_PGR)), static_cast<V const*>(ax), static_cast<V const*>(dg), th);
+          V const tp = static_cast<V>(wdot<MIXED>(th, ax, M));
           R nl = 0;
           for (int e = lane; e < M; e += 32) {
             th[e] -= tp * ax[e];
             nl += static_cast<R>(th[e]) * static_cast<R>(th[e]);
           }
           double const nn = wsum<MIXED>(nl);
-          double const inv = scal<MIXED>([&] { return rsqrtf(static_cast<float>(nn)); }, [&] { return 1 / sqrt(nn); });
+          V const inv = static_cast<V>(scal<MIXED>([&] { return rsqrtf(static_cast<float>(nn)); },
+                                                   [&] { return 1 / sqrt(nn); }));
           R bl = 0, cl = 0;
           for (int e = lane; e < M; e += 32) {
             th[e] *= inv;
-            double const df = g1[e] - g0[e];
+            V const df = g1[e] - g0[e];
             bl += static_cast<R>(df) * static_cast<R>(th[e]);
             cl += static_cast<R>(df) * static_cast<R>(ax[e]);
           }
@@ -1152,7 +1176,7 @@ namespace flygpu {
           b_1 = scal<MIXED>([&] { return static_cast<float>(b) / static_cast<float>(dr); }, [&] { return b / dr; });
           c_x0 = scal<MIXED>([&] { return static_cast<float>(cc) / static_cast<float>(dr); }, [&] { return cc / dr; });
           double const b1 = b_1, cx0 = c_x0;
-          if (MIXED) {  // rotation angles in binary32 (see rotor_angles)
+          if (MIXED) {  // rotation angles in binary32 (see below)
             theta_1 = -0.5 * static_cast<double>(atanf(static_cast<float>(b1) / fabsf(static_cast<float>(cx0))));
           } else {
             theta_1 = lane0([&] { return -0.5 * atan(b1 / fabs(cx0)); });
@@ -1162,81 +1186,82 @@ namespace flygpu {
             act = ACT_STOP;
           } else {
             double const t1 = theta_1;
-            double c1, s1;
+            V c1, s1;
             if (MIXED) {
               float sf, cf;
               sincosf(static_cast<float>(t1), &sf, &cf);
-              c1 = cf;
-              s1 = sf;
+              c1 = static_cast<V>(cf);
+              s1 = static_cast<V>(sf);
             } else {
-              c1 = lane0([&] { return cos(t1); });
-              s1 = lane0([&] { return sin(t1); });
+              c1 = static_cast<V>(lane0([&] { return cos(t1); }));
+              s1 = static_cast<V>(lane0([&] { return sin(t1); }));
             }
             for (int e = lane; e < M; e += 32) {
               axp[e] = ax[e] * c1 + th[e] * s1;
-              double const nd = -dr * axp[e];
-              double const upd = nd - dprev[e];
+              V const nd = -drv * axp[e];
+              V const upd = nd - dprev[e];
               dprev[e] = nd;
-              comp(c.xl[c.aatom[e / 3]], e % 3) -= upd;
+              comp(c.xl[c.aatom[e / 3]], e % 3) -= static_cast<double>(upd);
             }
           }
         }
         if (block_action(sh, act) == ACT_STOP) break;
         if (gradient<MIXED, LPA>(c, tb, sh, g1p)) return true;
         if (lead) {
-          Red<MIXED> cxl = 0;
-          for (int e = lane; e < M; e += 32)
-            cxl += static_cast<Red<MIXED>>(g1p[e] - g0[e]) * static_cast<Red<MIXED>>(axp[e]);
+          R cxl = 0;
+          for (int e = lane; e < M; e += 32) cxl += static_cast<R>(g1p[e] - g0[e]) * static_cast<R>(axp[e]);
           double const cx = wsum<MIXED>(cxl);
           double const t1 = theta_1, b1 = b_1, cx0 = c_x0;
-          // the rotor's scalar trigonometry (rotor.cpp:120-134) on lane 0, broadcast as a block
+          // the rotor's scalar trigonometry (rotor.cpp:120-134)
           double sc[6];
           if (MIXED) {
-            // Rotor angles in binary32: the curvatures c_x0, c_x1 and b_1 come from binary64 dots; the
+            // Rotor angles in binary32: the curvatures c_x0, c_x1 and b_1 come from the dots above; the
             // angle arithmetic of rotor.cpp:120-134 is carried in binary32 (errors ~1e-7 rad, far below
             // the rotor's angle tolerance), with 1 - cos(2x) written as 2 sin^2(x) to keep its precision.
-            double const c_x1 = cx / dr;
+            float const c_x1 = static_cast<float>(cx) / static_cast<float>(dr);
             float const f1 = static_cast<float>(t1);
             float s1f, c1f, s2f, c2f;
             sincosf(f1, &s1f, &c1f);
             sincosf(2.f * f1, &s2f, &c2f);
-            double const a_1 = (cx0 - c_x1 + b1 * static_cast<double>(s2f)) / (2.0 * static_cast<double>(s1f) * static_cast<double>(s1f));
-            float tm = 0.5f * atanf(static_cast<float>(b1 / a_1));
+            float const a_1 = (static_cast<float>(cx0) - c_x1 + static_cast<float>(b1) * s2f) / (2.f * s1f * s1f);
+            float tm = 0.5f * atanf(static_cast<float>(b1) / a_1);
             float sm2, cm2;
             sincosf(2.f * tm, &sm2, &cm2);
             float const sm1 = sinf(tm);
-            if (-2.0 * a_1 * static_cast<double>(sm1) * static_cast<double>(sm1) + b1 * static_cast<double>(sm2) > 0) tm += 1.57079632679489661923f;
+            if (-2.f * a_1 * sm1 * sm1 + static_cast<float>(b1) * sm2 > 0.f) tm += 1.57079632679489661923f;
             float smf, cmf;
             sincosf(tm, &smf, &cmf);
             sc[0] = cmf;
             sc[1] = smf;
             sc[2] = sinf(f1 - tm) / s1f;
             sc[3] = smf / s1f;
-            sc[4] = 1.0 - static_cast<double>(cmf) - static_cast<double>(smf) * static_cast<double>(tanf(0.5f * f1));
+            sc[4] = 1.f - cmf - smf * tanf(0.5f * f1);
             sc[5] = tm;
-          } else if (lane == 0) {
-            double const c_x1 = cx / dr;
-            double const a_1 = (cx0 - c_x1 + b1 * sin(2 * t1)) / (1 - cos(2 * t1));
-            double theta_min = 0.5 * atan(b1 / a_1);
-            if (a_1 * cos(2 * theta_min) - a_1 + b1 * sin(2 * theta_min) > 0) theta_min += M_PI / 2;
-            double const cm = cos(theta_min), sm = sin(theta_min);
-            sc[0] = cm;
-            sc[1] = sm;
-            sc[2] = sin(t1 - theta_min) / sin(t1);
-            sc[3] = sm / sin(t1);
-            sc[4] = 1 - cm - sm * tan(0.5 * t1);
-            sc[5] = theta_min;
-          }
-          if (!MIXED) {
+          } else {
+            if (lane == 0) {
+              double const c_x1 = cx / dr;
+              double const a_1 = (cx0 - c_x1 + b1 * sin(2 * t1)) / (1 - cos(2 * t1));
+              double theta_min = 0.5 * atan(b1 / a_1);
+              if (a_1 * cos(2 * theta_min) - a_1 + b1 * sin(2 * theta_min) > 0) theta_min += M_PI / 2;
+              double const cm = cos(theta_min), sm = sin(theta_min);
+              sc[0] = cm;
+              sc[1] = sm;
+              sc[2] = sin(t1 - theta_min) / sin(t1);
+              sc[3] = sm / sin(t1);
+              sc[4] = 1 - cm - sm * tan(0.5 * t1);
+              sc[5] = theta_min;
+            }
 #pragma unroll
             for (int q = 0; q < 6; ++q) sc[q] = __shfl_sync(FULL, lane == 0 ? sc[q] : 0.0, 0);
           }
-          double const cm = sc[0], sm = sc[1], w1 = sc[2], w1p = sc[3], w0 = sc[4], theta_min = sc[5];
-          Red<MIXED> ql = 0;
+          V const cm = static_cast<V>(sc[0]), sm = static_cast<V>(sc[1]), w1 = static_cast<V>(sc[2]),
+                  w1p = static_cast<V>(sc[3]), w0 = static_cast<V>(sc[4]);
+          double const theta_min = sc[5];
+          R ql = 0;
           for (int e = lane; e < M; e += 32) {
             ax[e] = ax[e] * cm + th[e] * sm;
             g1[e] = w1 * g1[e] + w1p * g1p[e] + w0 * g0[e];
-            ql += static_cast<Red<MIXED>>(g1[e] - g0[e]) * static_cast<Red<MIXED>>(ax[e]);
+            ql += static_cast<R>(g1[e] - g0[e]) * static_cast<R>(ax[e]);
           }
           __syncwarp();
           if (fabs(theta_min) < o.theta_tol) {
@@ -1249,9 +1274,9 @@ namespace flygpu {
       }
       if (lead) {
         wlist_update(c, dprev, -1.0);  // xl -= -dprev: back to the centre
-        double const p = wdot<MIXED>(g0, ax, M);
+        V const p = static_cast<V>(wdot<MIXED>(g0, ax, M));
         bool const parallel_only = !o.relax_in_convex && curv > 0;
-        for (int e = lane; e < M; e += 32) eff[e] = parallel_only ? -p * ax[e] : g0[e] - 2 * p * ax[e];
+        for (int e = lane; e < M; e += 32) eff[e] = parallel_only ? -p * ax[e] : g0[e] - V(2) * p * ax[e];
         __syncwarp();
         if (c.S->count_frozen == 0) trans_proj(c, eff);
         if (lane == 0) sh.curv = curv;
@@ -1261,6 +1286,27 @@ namespace flygpu {
     }
 
     // ------------------------------------------------------------------ one search
+
+    // Binary32-pair searches keep the axis in binary32 (Vt) while they run; the host writes and reads it
+    // in binary64. Converts the V_AX slot in place (to_v: binary64 -> V, else V -> binary64) through the
+    // V_G0 slot, which holds no state at the start or the end of a search. All threads.
+    template <bool MIXED>
+    __device__ void axis_storage(Ctx const& c, bool to_v) {
+      double* axd = c.V(V_AX);
+      double* tmp = c.V(V_G0);
+      Vt<MIXED>* axv = vp<MIXED>(axd);
+      __syncthreads();
+      for (int e = threadIdx.x; e < c.M; e += blockDim.x) tmp[e] = to_v ? axd[e] : static_cast<double>(axv[e]);
+      __syncthreads();
+      for (int e = threadIdx.x; e < c.M; e += blockDim.x) {
+        if (to_v) {
+          axv[e] = static_cast<Vt<MIXED>>(tmp[e]);
+        } else {
+          axd[e] = tmp[e];
+        }
+      }
+      __syncthreads();
+    }
 
     template <bool MIXED, int LPA>
     __device__ void run(BatchView const& bv, Blk& sh, Ctx& cs, int sidx) {
@@ -1335,9 +1381,10 @@ namespace flygpu {
       Ctx const& c = cs;
       TablesView const& tb = bv.tb;
       double const skin = S->rc_list - (dimer ? o.r_cut + 2 * o.delta_r : o.r_cut);
+      using V = Vt<MIXED>;
       double* X = c.V(V_X);
-      double* eff = c.V(V_EFF);
-      double* hg = c.V(V_HG);
+      V* eff = vp<MIXED>(c.V(V_EFF));
+      V* hg = vp<MIXED>(c.V(V_HG));
       int const M = c.M;
       bool const lead = threadIdx.x < 32;
       int const lane = threadIdx.x & 31;
@@ -1362,6 +1409,7 @@ namespace flygpu {
           pack_one(c, i);
           c.dacc[i] = 0;
         }
+        if (MIXED && dimer) axis_storage<true>(c, true);  // the host wrote the axis in binary64
         err = rebuild(c, sh, S->rc_list);
         static_density<MIXED>(c, tb, sh);
         __syncthreads();
@@ -1433,16 +1481,17 @@ namespace flygpu {
             }
           }
           if (act == ACT_GO) {
-            newton<MIXED>(c, c.mT, kT, c.sT(0), c.yT(0), sh.rhoT, sh.alphaT, c.V(V_PXT), c.V(V_PGT), X, eff, hg);
+            newton<MIXED>(c, c.mT, kT, c.sT(0), c.yT(0), sh.rhoT, sh.alphaT, c.V(V_PXT), vp<MIXED>(c.V(V_PGT)),
+                          static_cast<double const*>(X), static_cast<V const*>(eff), hg);
             double const nrm = wdot<MIXED>(hg, hg, M);
             double const tr = trust;
-            double const sc = scal<MIXED>([&] { return fminf(1.f, static_cast<float>(tr) * rsqrtf(static_cast<float>(nrm))); },
-                                          [&] { return fmin(1.0, tr / sqrt(nrm)); });
+            V const sc = static_cast<V>(scal<MIXED>([&] { return fminf(1.f, static_cast<float>(tr) * rsqrtf(static_cast<float>(nrm))); },
+                                                    [&] { return fmin(1.0, tr / sqrt(nrm)); }));
             Red<MIXED> hl = 0;
             for (int e = lane; e < M; e += 32) {
               hg[e] *= sc;
               hl += static_cast<Red<MIXED>>(hg[e]) * static_cast<Red<MIXED>>(hg[e]);
-              X[e] -= hg[e];
+              X[e] -= static_cast<double>(hg[e]);
             }
             double const hh = wsum<MIXED>(hl);
             acc += scal<MIXED>([&] { return sqrtf(static_cast<float>(hh)); }, [&] { return sqrt(hh); });
@@ -1502,6 +1551,7 @@ namespace flygpu {
         }
       }
       __syncthreads();
+      if (MIXED && dimer && (done || err)) axis_storage<true>(c, false);  // the host reads it in binary64
       if (st_v) {
         for (std::size_t e = threadIdx.x; e < vb; e += blockDim.x) S->vec[e] = c.v[e];
       }
