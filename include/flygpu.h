@@ -201,6 +201,12 @@ int flygpu_batch_run(flygpu_batch* batch, const flygpu_tuning* tuning);
 int flygpu_batch_autotune(flygpu_batch* batch, flygpu_tuning* best);
 /* Restores every search's inputs so the batch can run again. */
 int flygpu_batch_reset(flygpu_batch* batch);
+/* Two-phase runs (the default: 100 steps, wide = {1, 256, 1, 0}): flygpu_batch_run first runs every
+ * search for at most `steps` translation steps in the throughput shape, then the unfinished ones to
+ * completion in the `wide` shape (one CTA per search with more threads: lower latency per step).
+ * steps <= 0: one launch. wide NULL keeps the current wide shape. No reference counterpart (the
+ * reference runs one search per OpenMP task, saddle/find.cpp:697-731). */
+int flygpu_batch_set_stragglers(flygpu_batch* batch, int steps, const flygpu_tuning* wide);
 /* Waits for the batch and copies results; pos_out / axis_out (sum of 3n) may be NULL. */
 int flygpu_batch_results(flygpu_batch* batch, flygpu_search_result* results, double* pos_out, double* axis_out);
 int64_t flygpu_batch_device_bytes(const flygpu_batch* batch);

@@ -41,7 +41,39 @@ namespace flygpu {
       }
     }
 
+    // Ordered compaction of the unfinished items (one CTA of 1024 threads, ballot prefix sums).
+    __global__ void k_unfinished(SearchDev const* __restrict__ S, int const* __restrict__ order, int n,
+                                 int* __restrict__ out, int* __restrict__ n_out) {
+      __shared__ int base;
+      __shared__ int wcount[32];
+      int const lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+      if (threadIdx.x == 0) base = 0;
+      __syncthreads();
+      for (int k0 = 0; k0 < n; k0 += blockDim.x) {
+        int const k = k0 + threadIdx.x;
+        bool const keep = k < n && S[order[k]].stage != STAGE_DONE;
+        unsigned const bal = __ballot_sync(0xffffffffu, keep);
+        if (lane == 0) wcount[w] = __popc(bal);
+        __syncthreads();
+        int off = base;
+        for (int q = 0; q < w; ++q) off += wcount[q];
+        if (keep) out[off + __popc(bal & ((1u << lane) - 1u))] = order[k];
+        __syncthreads();
+        if (threadIdx.x == 0) {
+          int t = 0;
+          for (int q = 0; q < nw; ++q) t += wcount[q];
+          base += t;
+        }
+        __syncthreads();
+      }
+      if (threadIdx.x == 0) *n_out = base;
+    }
+
   }  // namespace
+
+  void search_unfinished(SearchDev const* S, int const* order, int n, int* order_out, int* n_out, cudaStream_t s) {
+    launch(k_unfinished, 1, 1024, 0, s, S, order, n, order_out, n_out);
+  }
 
   SearchLayout search_layout(int n, int na, int n_vec_doubles, int n_hist_doubles) {
     auto up = [](std::size_t b) { return (b + 255) / 256 * 256; };

@@ -131,6 +131,9 @@ namespace flygpu {
   void search_init_kernels();
   SearchLayout search_layout(int n, int na, int n_vec_doubles, int n_hist_doubles);
   void search_bind(SearchDev& S, char* base, SearchLayout const& l);
+  // The items of order[0..n) whose search has not finished, in the same order, into order_out, and
+  // their count into *n_out (device memory). One CTA.
+  void search_unfinished(SearchDev const* S, int const* order, int n, int* order_out, int* n_out, cudaStream_t s);
 
   // search_host.cpp: fill one search's state and initial arrays (image at byte `at` of img).
   SearchLayout search_prepare(SearchOpts const& o, int n_types, flygpu_search_desc const& d, SearchDev& S,

@@ -91,16 +91,22 @@ struct flygpu_batch {
   std::int64_t total_atoms = 0, total_act = 0;
   std::size_t block_bytes = 0;
   int smem_bytes = 0;  // dynamic shared memory per CTA for staging searches (search_smem_need, capped)
+  // Two-phase runs: the whole batch for straggler_steps translation steps with the throughput shape,
+  // then the unfinished searches with the wide (low-latency) shape. straggler_steps <= 0: one phase.
+  int straggler_steps = 100;
+  flygpu_tuning wide{1, 256, 1, 0};
+  DevBuf<int> order2, n2;
   bool tuned = false;
   flygpu_tuning tuning{};
   std::string tune_key;
 
-  BatchView view(int const* ord, int n_items, int budget) {
+  BatchView view(int const* ord, int n_items, int budget, int const* n_items_dev = nullptr) {
     BatchView v{};
     v.S = S.p;
     v.n_search = n_search;
     v.order = ord;
     v.n_items = n_items;
+    v.n_items_dev = n_items_dev;
     v.work = work.p;
     v.budget = budget;
     v.smem_bytes = smem_bytes;
@@ -311,6 +317,8 @@ namespace flygpu {
     B->out_x.reserve(static_cast<std::size_t>(3 * act));
     B->out_ax.reserve(static_cast<std::size_t>(3 * act));
     B->work.reserve(1);
+    B->order2.reserve(static_cast<std::size_t>(n_search));
+    B->n2.reserve(1);
     FLY_CUDA(cudaStreamSynchronize(st));
     B->bytes = static_cast<std::int64_t>(B->S.n * sizeof(SearchDev) + 2 * off + 2 * B->out_x.n * 8);
     // autotune cache key: device, precision and the size bucket of the batch
@@ -333,12 +341,27 @@ namespace flygpu {
     FLY_CUDA(cudaMemcpyAsync(B->block.p, B->block_init.p, B->block_bytes, cudaMemcpyDeviceToDevice, st));
   }
 
-  void batch_launch(flygpu_batch* B, flygpu_tuning const& t, int const* ord, int n_items, int budget) {
+  // n_items_dev: if set, the item count is read on the device (n_items is then an upper bound).
+  void batch_launch(flygpu_batch* B, flygpu_tuning const& t, int const* ord, int n_items, int budget,
+                    int const* n_items_dev = nullptr) {
     if (t.threads % 32 || t.threads < 32 || t.threads > 1024) fail(FLYGPU_INVALID_ARG, "bad threads per CTA");
     int const blocks = std::max(1, std::min(n_items, std::max(1, t.blocks_per_sm) * sm_count()));
     FLY_CUDA(cudaMemsetAsync(B->work.p, 0, sizeof(int), B->stream));
-    search_launch(B->view(ord, n_items, budget), t.lanes_per_atom, t.threads, t.max_registers, blocks, B->mixed,
-                  B->stream);
+    search_launch(B->view(ord, n_items, budget, n_items_dev), t.lanes_per_atom, t.threads, t.max_registers, blocks,
+                  B->mixed, B->stream);
+  }
+
+  // Every search of the batch to completion: one launch, or (straggler_steps > 0) a budgeted launch of
+  // the whole batch followed by one of its unfinished searches in the wide shape. A search's long tail
+  // then runs at the wide shape's lower latency per step instead of holding one narrow CTA.
+  void batch_run_all(flygpu_batch* B, flygpu_tuning const& t) {
+    if (B->straggler_steps <= 0) {
+      batch_launch(B, t, B->order_d.p, B->n_search, 0);
+      return;
+    }
+    batch_launch(B, t, B->order_d.p, B->n_search, B->straggler_steps);
+    search_unfinished(B->S.p, B->order_d.p, B->n_search, B->order2.p, B->n2.p, B->stream);
+    batch_launch(B, B->wide, B->order2.p, B->n_search, 0, B->n2.p);
   }
 
   flygpu_tuning autotune(flygpu_batch* B) {
@@ -370,7 +393,7 @@ namespace flygpu {
           t.blocks_per_sm = std::max(1, bps);
           batch_reset(B);
           FLY_CUDA(cudaEventRecord(e0, B->stream));
-          batch_launch(B, t, ord.p, want, 0);
+          batch_launch(B, t, ord.p, want, B->straggler_steps);  // the throughput phase
           FLY_CUDA(cudaEventRecord(e1, B->stream));
           FLY_CUDA(cudaEventSynchronize(e1));
           float ms = 0;
@@ -475,7 +498,18 @@ int flygpu_batch_run(flygpu_batch* B, const flygpu_tuning* tuning) {
       }
       t = B->tuning;
     }
-    batch_launch(B, t, B->order_d.p, B->n_search, 0);
+    batch_run_all(B, t);
+  });
+}
+
+int flygpu_batch_set_stragglers(flygpu_batch* B, int steps, const flygpu_tuning* wide) {
+  return guard([&] {
+    if (!B) fail(FLYGPU_INVALID_ARG, "null batch");
+    if (wide && (wide->threads % 32 || wide->threads < 64 || wide->threads > 1024))
+      fail(FLYGPU_INVALID_ARG, "bad threads per CTA");
+    B->straggler_steps = steps;
+    if (wide) B->wide = *wide;
+    B->tuned = false;  // the throughput phase is tuned with the budget
   });
 }
 

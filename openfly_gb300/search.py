@@ -100,6 +100,7 @@ def _setup() -> None:
     L.flygpu_batch_run.argtypes = [V, V]
     L.flygpu_batch_autotune.argtypes = [V, V]
     L.flygpu_batch_reset.argtypes = [V]
+    L.flygpu_batch_set_stragglers.argtypes = [V, C.c_int, V]
     L.flygpu_batch_results.argtypes = [V, V, V, V]
     L.flygpu_batch_device_bytes.restype = C.c_int64
     L.flygpu_batch_device_bytes.argtypes = [V]
@@ -190,6 +191,12 @@ class Batch:
 
     def reset(self) -> None:
         check(lib().flygpu_batch_reset(self.h), "Batch.reset")
+
+    def set_stragglers(self, steps: int, wide: Tuning | None = None) -> None:
+        """Two-phase runs (flygpu_batch_set_stragglers): `steps` translation steps for the whole batch in
+        the throughput shape, then the unfinished searches in the `wide` shape; steps <= 0: one launch."""
+        check(lib().flygpu_batch_set_stragglers(self.h, int(steps), C.byref(wide) if wide is not None else None),
+              "Batch.set_stragglers")
 
     @property
     def device_bytes(self) -> int:

@@ -84,6 +84,22 @@ def test_batched_dimer_matches_oracle(gpu, oracle, odata, geam, search_mod, clus
         assert abs(r["energy"] - oracle_energy(O, odata, c.sys, p)) < 1e-4
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_two_phase_run_matches_oracle(gpu, oracle, odata, geam, search_mod, clusters, oracle_refs, precision):
+    # Every search stops after one translation step in the throughput shape and resumes, from its saved
+    # state, in the wide shape; one-phase runs (steps 0) are the single persistent launch.
+    S, O = search_mod, oracle
+    gopt, oopt = c3_options(S, O)
+    prec = gpu.FP64 if precision == "fp64" else gpu.MIXED
+    for steps in (1, 0):
+        b = S.Batch(geam, [S.from_cluster(c) for c in clusters], precision=prec, dimer=gopt)
+        b.set_stragglers(steps, S.Tuning(1, 256, 1, 0))
+        b.run(S.Tuning(4, 128, 2))
+        res, pos, ax = b.results()
+        assert all(r["status"] == 0 for r in res), res
+        compare(res, oracle_refs, f"{precision} stragglers {steps}", positions=pos)
+
+
 def test_same_alone_and_in_mix(gpu, geam, search_mod, clusters):
     S = search_mod
     gopt = S.DimerOptions.defaults(n=6, rot_n=6, f2norm=1e-3)
