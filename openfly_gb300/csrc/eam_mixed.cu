@@ -8,8 +8,12 @@
 //   * pair terms are summed in binary32 over runs of at most CHUNK consecutive neighbours and each run
 //     is added to the atom's binary64 accumulator (density, pair energy, gradient).
 // F(rho) and F'(rho) are per-atom and evaluated in binary64 from the binary64 table.
+// Both passes are bound by L1/TEX gathers, so each pair reads its neighbour's 32-byte slot record and
+// one merged 32-byte spline record (phi and v of the ordered type pair) with one 256-bit load each; the
+// force pass reads a second merged record only for pairs of different types (phi of the other order).
 
 #include "internal.hpp"
+#include "ld256.cuh"
 
 namespace flygpu {
 
@@ -65,22 +69,25 @@ namespace flygpu {
           int const k1 = min(cnt, k0 + CHUNK);
           for (int k = k0; k < k1; ++k) {
             int const q = nbr[static_cast<std::int64_t>(k) * n + j];
-            Packed const o = pk[q];
-            float const dx = (o.hx - me.hx) + (o.lx - me.lx);
-            float const dy = (o.hy - me.hy) + (o.ly - me.ly);
-            float const dz = (o.hz - me.hz) + (o.lz - me.lz);
+            float4 oh, ol;  // (hx, hy, hz, type bits), (lx, ly, lz, fp)
+            ld256(pk + q, oh, ol);
+            float const dx = (oh.x - me.hx) + (ol.x - me.lx);
+            float const dy = (oh.y - me.hy) + (ol.y - me.ly);
+            float const dz = (oh.z - me.hz) + (ol.z - me.lz);
             float const r2 = dx * dx + dy * dy + dz * dz;
             if (r2 < rc2) {
               float const r = sqrtf(r2);
-              int const tq = static_cast<int>(o.type);
+              int const tq = __float_as_int(oh.w);
               int i;
               float t;
               if (!fetch32(r, tb.finv_dR, tb.nR, i, t)) {
                 bad = true;
                 continue;
               }
-              rho_f += f32(__ldg(&tb.phi32[static_cast<std::int64_t>(tq + nt * ti) * tb.nR + i]), t);
-              if (ENERGY) v_f += f32(__ldg(&tb.v32[static_cast<std::int64_t>(ti + nt * tq) * tb.nR + i]), t);
+              float4 cphi, cv;
+              ld256(tb.pv32 + static_cast<std::int64_t>(ti * nt + tq) * tb.nR + i, cphi, cv);
+              rho_f += f32(cphi, t);
+              if (ENERGY) v_f += f32(cv, t);
             }
           }
           rho += static_cast<double>(rho_f);
@@ -142,25 +149,35 @@ namespace flygpu {
           float fx = 0.f, fy = 0.f, fz = 0.f;
           for (int k = k0; k < k1; ++k) {
             int const q = nbr[static_cast<std::int64_t>(k) * n + j];
-            Packed const o = pk[q];
-            float const dx = (o.hx - me.hx) + (o.lx - me.lx);
-            float const dy = (o.hy - me.hy) + (o.ly - me.ly);
-            float const dz = (o.hz - me.hz) + (o.lz - me.lz);
+            float4 oh, ol;  // (hx, hy, hz, type bits), (lx, ly, lz, fp)
+            ld256(pk + q, oh, ol);
+            float const dx = (oh.x - me.hx) + (ol.x - me.lx);
+            float const dy = (oh.y - me.hy) + (ol.y - me.ly);
+            float const dz = (oh.z - me.hz) + (ol.z - me.lz);
             float const r2 = dx * dx + dy * dy + dz * dz;
             if (r2 < rc2) {
               float const ir = rsqrtf(r2);
               float const r = r2 * ir;
-              int const tq = static_cast<int>(o.type);
+              int const tq = __float_as_int(oh.w);
               int i;
               float t;
               if (!fetch32(r, inv, tb.nR, i, t)) {
                 bad = true;
                 continue;
               }
-              float const dv = dfdt32(__ldg(&tb.v32[static_cast<std::int64_t>(tq + nt * ti) * tb.nR + i]), t);
-              float const dphi_qi = dfdt32(__ldg(&tb.phi32[static_cast<std::int64_t>(tq + nt * ti) * tb.nR + i]), t);
-              float const dphi_iq = dfdt32(__ldg(&tb.phi32[static_cast<std::int64_t>(ti + nt * tq) * tb.nR + i]), t);
-              float const s = (dv + me.fp * dphi_qi + o.fp * dphi_iq) * inv * ir;
+              // phi_{q->i} and v from the (t_i, t_q) record; phi_{i->q} is the same function when the
+              // types agree, else the phi of the (t_q, t_i) record (v is symmetric in the types)
+              float4 cphi, cv;
+              ld256(tb.pv32 + static_cast<std::int64_t>(ti * nt + tq) * tb.nR + i, cphi, cv);
+              float4 cphi_o = cphi;
+              if (tq != ti) {
+                float4 unused;
+                ld256(tb.pv32 + static_cast<std::int64_t>(tq * nt + ti) * tb.nR + i, cphi_o, unused);
+              }
+              float const dv = dfdt32(cv, t);
+              float const dphi_qi = dfdt32(cphi, t);
+              float const dphi_iq = dfdt32(cphi_o, t);
+              float const s = (dv + me.fp * dphi_qi + ol.w * dphi_iq) * inv * ir;
               fx -= s * dx;
               fy -= s * dy;
               fz -= s * dz;

@@ -134,6 +134,13 @@ namespace flygpu {
     DevBuf<float4> d32;
   };
 
+  // Merged binary32 spline record of one (receiver type t_i, neighbour type t_n, interval): phi of the
+  // neighbour's type at the receiver (phi_{t_n -> t_i}, the reference's phi[t_n + n t_i]) and the pair
+  // potential v_{t_i t_n}, both in the interval's unit coordinate. 32 bytes: one sector, one 256-bit load.
+  struct alignas(32) PairRec {
+    float4 phi, v;
+  };
+
   // Device view passed to kernels by value.
   struct TablesView {
     int n_types;
@@ -146,6 +153,7 @@ namespace flygpu {
     float4 const* F32;
     float4 const* phi32;
     float4 const* v32;
+    PairRec const* pv32;  // [t_i * n_types + t_n] * nR + interval
   };
 
 }  // namespace flygpu
@@ -156,6 +164,7 @@ struct flygpu_eam {
   std::vector<std::string> names;
   std::vector<double> mass;
   flygpu::SplineSet F, phi, v;  // phi and v hold n*n functions (v symmetric, both orders)
+  flygpu::DevBuf<flygpu::PairRec> pv;  // phi and v of each ordered type pair merged per interval
   flygpu::TablesView view() const;
 };
 

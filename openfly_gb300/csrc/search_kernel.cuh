@@ -301,7 +301,7 @@ namespace flygpu {
         for (int u = 0; u < U; ++u) o[u] = c.pk[j[u] < 0 ? i : j[u]];
         float dx[U], dy[U], dz[U], ir[U], tt[U];
         std::int64_t rij[U], rji[U];
-        bool use[U];
+        bool use[U], same[U];
 #pragma unroll
         for (int u = 0; u < U; ++u) {
           dx[u] = (o[u].hx - me.hx) + (o[u].lx - me.lx);
@@ -317,17 +317,22 @@ namespace flygpu {
           int const ii = use[u] ? static_cast<int>(x) : 0;
           tt[u] = x - static_cast<float>(ii);
           int const tj = static_cast<int>(o[u].type & TYPE_MASK);
-          rij[u] = static_cast<std::int64_t>(tj + nty * ti) * tb.nR + ii;
-          rji[u] = static_cast<std::int64_t>(ti + nty * tj) * tb.nR + ii;
+          same[u] = tj == ti;
+          rij[u] = static_cast<std::int64_t>(ti * nty + tj) * tb.nR + ii;  // merged (t_i, t_j) record
+          rji[u] = static_cast<std::int64_t>(tj * nty + ti) * tb.nR + ii;  // merged (t_j, t_i) record
         }
+        // (t_i, t_j) record: phi_{j->i} and v; phi_{i->j} is the same function for equal types, else the
+        // phi of the (t_j, t_i) record
+        // (128-bit loads: ptxas of CUDA 13.0 fails on the 256-bit form in the register-capped variant)
         float4 cv[U], ca[U], cb[U];
         float4 const z4 = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
         for (int u = 0; u < U; ++u) {
-          cv[u] = use[u] ? __ldg(&tb.v32[rij[u]]) : z4;
-          ca[u] = use[u] ? __ldg(&tb.phi32[rij[u]]) : z4;
-          cb[u] = use[u] ? __ldg(&tb.phi32[rji[u]]) : z4;
+          ca[u] = use[u] ? __ldg(&tb.pv32[rij[u]].phi) : z4;
+          cv[u] = use[u] ? __ldg(&tb.pv32[rij[u]].v) : z4;
         }
+#pragma unroll
+        for (int u = 0; u < U; ++u) cb[u] = use[u] && !same[u] ? __ldg(&tb.pv32[rji[u]].phi) : ca[u];
 #pragma unroll
         for (int u = 0; u < U; ++u) {
           float const t = tt[u];
@@ -563,7 +568,7 @@ namespace flygpu {
         for (int u = 0; u < U; ++u) o[u] = c.pk[j[u] < 0 ? i : j[u]];
         float tt[U];
         std::int64_t rown[U], rowo[U];
-        bool use[U], stat[U];
+        bool use[U], stat[U], same[U];
 #pragma unroll
         for (int u = 0; u < U; ++u) {
           float const dx = (o[u].hx - me.hx) + (o[u].lx - me.lx);
@@ -579,16 +584,16 @@ namespace flygpu {
           int const ii = use[u] ? static_cast<int>(x) : 0;
           tt[u] = x - static_cast<float>(ii);
           int const tj = static_cast<int>(o[u].type & TYPE_MASK);
-          rown[u] = static_cast<std::int64_t>(tj + nty * ti) * tb.nR + ii;
-          rowo[u] = static_cast<std::int64_t>(ti + nty * tj) * tb.nR + ii;
+          same[u] = tj == ti;
+          rown[u] = static_cast<std::int64_t>(ti * nty + tj) * tb.nR + ii;  // merged (t_i, t_j): phi_{j->i}
+          rowo[u] = static_cast<std::int64_t>(tj * nty + ti) * tb.nR + ii;  // merged (t_j, t_i): phi_{i->j}
         }
         float4 cp[U], cq[U];
         float4 const z4 = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
-        for (int u = 0; u < U; ++u) {
-          cp[u] = use[u] ? __ldg(&tb.phi32[rown[u]]) : z4;
-          cq[u] = stat[u] ? __ldg(&tb.phi32[rowo[u]]) : z4;
-        }
+        for (int u = 0; u < U; ++u) cp[u] = use[u] ? __ldg(&tb.pv32[rown[u]].phi) : z4;
+#pragma unroll
+        for (int u = 0; u < U; ++u) cq[u] = stat[u] && !same[u] ? __ldg(&tb.pv32[rowo[u]].phi) : cp[u];
 #pragma unroll
         for (int u = 0; u < U; ++u) {
           float const t = tt[u];

@@ -73,7 +73,8 @@ namespace flygpu {
       return raw;
     }
 
-    void upload(SplineSet& s) {
+    // Binary32 coefficients of every interval in its unit coordinate.
+    std::vector<float4> unit32(SplineSet const& s) {
       std::size_t const total = static_cast<std::size_t>(s.count) * static_cast<std::size_t>(s.n_spines);
       std::vector<float4> f32(total);
       for (std::size_t k = 0; k < total; ++k) {
@@ -82,6 +83,12 @@ namespace flygpu {
         f32[k] = make_float4(static_cast<float>(c[0]), static_cast<float>(c[1] * dx),
                              static_cast<float>(c[2] * dx * dx), static_cast<float>(c[3] * dx * dx * dx));
       }
+      return f32;
+    }
+
+    void upload(SplineSet& s) {
+      std::size_t const total = static_cast<std::size_t>(s.count) * static_cast<std::size_t>(s.n_spines);
+      std::vector<float4> const f32 = unit32(s);
       s.d64.reserve(total);
       s.d32.reserve(total);
       FLY_CUDA(cudaMemcpy(s.d64.p, s.host.data(), total * sizeof(D4), cudaMemcpyHostToDevice));
@@ -111,6 +118,7 @@ flygpu::TablesView flygpu_eam::view() const {
   t.F32 = F.d32.p;
   t.phi32 = phi.d32.p;
   t.v32 = v.d32.p;
+  t.pv32 = pv.p;
   return t;
 }
 
@@ -169,6 +177,22 @@ namespace flygpu {
     upload(E->F);
     upload(E->phi);
     upload(E->v);
+    {
+      // merged records: [t_i][t_n][interval] = {phi[t_n + n t_i], v[t_i + n t_n]}
+      int const nt = E->n_types;
+      std::size_t const nR = static_cast<std::size_t>(E->phi.n_spines);
+      std::vector<float4> const p32 = unit32(E->phi), v32 = unit32(E->v);
+      std::vector<PairRec> rec(static_cast<std::size_t>(nt) * static_cast<std::size_t>(nt) * nR);
+      for (int ti = 0; ti < nt; ++ti)
+        for (int tn = 0; tn < nt; ++tn)
+          for (std::size_t i = 0; i < nR; ++i) {
+            PairRec& r = rec[(static_cast<std::size_t>(ti) * nt + tn) * nR + i];
+            r.phi = p32[(static_cast<std::size_t>(tn) + static_cast<std::size_t>(nt) * ti) * nR + i];
+            r.v = v32[(static_cast<std::size_t>(ti) + static_cast<std::size_t>(nt) * tn) * nR + i];
+          }
+      E->pv.reserve(rec.size());
+      FLY_CUDA(cudaMemcpy(E->pv.p, rec.data(), rec.size() * sizeof(PairRec), cudaMemcpyHostToDevice));
+    }
     return E.release();
   }
 
