@@ -82,3 +82,38 @@ def test_empty_and_errors(gpu):
         gpu.List([2.0, 10.0, 10.0], [1, 1, 1], 3.0)  # r_cut larger than an extent (hypergrid.hpp:46-48)
     with pytest.raises(gpu.FlyGPUError):
         g.neighbours(3.5)  # r_cut above the list's cut-off (list.hpp:141-143)
+
+
+def test_dense_clump_regrows_capacity(gpu, oracle):
+    # The first neighbour capacity is sized from the mean density; a clump far denser than the mean
+    # overflows it, and the rebuild regrows the capacity once (as List grows its vectors, list.cpp:91-94).
+    rng = np.random.default_rng(3)
+    ext = np.array([20.0, 20.0, 20.0])
+    per = np.array([1, 0, 1], np.int32)
+    background = rng.random((1500, 3)) * ext
+    v = rng.normal(size=(200, 3))
+    clump = 10.0 + v / np.linalg.norm(v, axis=1, keepdims=True) * 1.5 * rng.random((200, 1)) ** (1 / 3)
+    pos = np.concatenate([background, clump])
+    rc = 3.0
+    g = gpu.List(ext, per, rc)
+    o = oracle.List(ext, per, rc)
+    g.rebuild(pos)
+    o.rebuild(pos, 1)
+    _same_lists(g.neighbours(rc), o.neighbours(rc))
+
+
+def test_tightest_periodic_box(gpu, oracle):
+    # Extents just above the cut-off in every periodic direction: the most ghosts per atom a valid
+    # box allows (about 26 per atom, under the reference's MAX_GHOST_RATIO capacity, list.hpp:78).
+    rng = np.random.default_rng(9)
+    rc = 3.0
+    ext = np.full(3, rc * 1.02)
+    per = np.ones(3, np.int32)
+    pos = rng.random((40, 3)) * ext
+    g = gpu.List(ext, per, rc)
+    o = oracle.List(ext, per, rc)
+    g.rebuild(pos)
+    o.rebuild(pos, 1)
+    assert g.num_ghosts == o.num_ghosts
+    assert g.num_ghosts > 20 * 40
+    _same_lists(g.neighbours(rc), o.neighbours(rc))
