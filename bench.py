@@ -190,7 +190,7 @@ def reference_arm(args):
         "impl": "reference", "metric": METRIC, "value": value, "unit": "atom-evals/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / k, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": config_dict(s, args),
+        "config": config_dict(s, args, reference=True),
         "cpu_baseline": {"value": value, "unit": "atom-evals/s", "cores": threads, "kind": "port",
                          "sample": f"{k} full steps ({rb} rebuilds) of the {s.n}-atom workload"},
         "e2e": {"value": value, "unit": "atom-evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -201,12 +201,18 @@ def reference_arm(args):
 METRIC = "saddle searches/s + p50/p99 latency vs one-at-a-time GPU @<=1 meV; atom-evals/s"
 
 
-def config_dict(s, args):
-    return {"workload": f"config 2: {args.cells}^3 bcc Fe, 0.1% vacancies, 0.05% H, sigma 0.05 A; per step "
-                        f"List::update (skin {SKIN} A, rebuild by the reference's skin rule) + EAM energy+gradient",
-            "atoms": s.n, "cells": args.cells, "precision": "binary32 pairs / binary64 accumulation",
-            "l2": "inputs larger than L2 (positions, packed slots, neighbour columns ~0.4 GB)",
-            "parallelism": f"replicas x{args.gpus}"}
+def config_dict(s, args, reference: bool = False):
+    c = {"workload": f"config 2: {args.cells}^3 bcc Fe, 0.1% vacancies, 0.05% H, sigma 0.05 A; per step "
+                     f"List::update (skin {SKIN} A, rebuild by the reference's skin rule) + EAM energy+gradient",
+         "atoms": s.n, "cells": args.cells}
+    if reference:
+        c.update({"precision": "binary64 (the reference's arithmetic, oracle port)",
+                  "parallelism": "host threads of rank 0"})
+    else:
+        c.update({"precision": "binary32 pairs / binary64 accumulation",
+                  "l2": "inputs larger than L2 (positions, packed slots, neighbour columns ~0.4 GB)",
+                  "parallelism": f"replicas x{args.gpus}"})
+    return c
 
 
 # ----------------------------------------------------------------------------- search metrics
