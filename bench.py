@@ -217,11 +217,49 @@ def config_dict(s, args, reference: bool = False):
 
 # ----------------------------------------------------------------------------- search metrics
 
+def serve_run(S, eam, stream, tune, opt, args, rate) -> dict:
+    """Config 4 through flygpu_server: submit `stream` with Poisson arrivals at `rate` per second (all at
+    once when rate is None) and poll completions on another thread; searches/s over the wall time from
+    the first submission to the last completion, latency from submission to completion."""
+    import threading
+
+    srv = S.Server(eam, hbm_budget_bytes=40 << 30, max_active=2048, steps_per_tick=args.steps_per_tick,
+                   tuning=tune, dimer=opt)
+    rng = np.random.default_rng(1)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, len(stream))) if rate else np.zeros(len(stream))
+    done: list = []
+    stop = threading.Event()
+
+    def poller():
+        while len(done) < len(stream) and not (stop.is_set() and len(done) >= len(stream)):
+            done.extend(srv.poll(512, wait_ms=20))
+            if stop.is_set() and srv.stats()["pending"] == 0 and srv.stats()["active"] == 0 and len(done) >= len(stream):
+                break
+
+    th = threading.Thread(target=poller)
+    th.start()
+    t0 = time.perf_counter()
+    for k, r in enumerate(stream):
+        while time.perf_counter() - t0 < arrivals[k]:
+            pass
+        srv.submit(r)
+    stop.set()
+    th.join(timeout=600)
+    elapsed = time.perf_counter() - t0
+    st = srv.stats()
+    srv.close()
+    lat = np.array([d["latency_ms"] for d in done])
+    ex = [d["exit_code"] for d in done]
+    return {"requests": len(stream), "completed": len(done), "arrival_rate_per_s": rate if rate else "all at once",
+            "searches_per_s": len(done) / elapsed, "p50_ms": float(np.percentile(lat, 50)),
+            "p99_ms": float(np.percentile(lat, 99)), "steps_per_tick": args.steps_per_tick, "ticks": st["ticks"],
+            "converged": ex.count(0), "hbm_budget_bytes": 40 << 30}
+
+
 def search_metrics(fly, args) -> dict:
     """Configs 3 and 4: batched searches/s (one persistent launch over 4096 clusters), the plain
     one-search-at-a-time drop-in GPU path on a sample, binary32-pair vs binary64 saddle energies, and
     the served path's searches/s with p50/p99 latency under Poisson arrivals."""
-    import threading
 
     import torch
 
@@ -282,42 +320,13 @@ def search_metrics(fly, args) -> dict:
                                              "p50_ms": float(np.percentile(lat, 50)),
                                              "p99_ms": float(np.percentile(lat, 99))}
     out["config3"]["batched_over_plain"] = out["config3"]["mixed"]["searches_per_s"] / plain
-    # served stream (config 4)
+    # served stream (config 4): Poisson arrivals at --arrival-rate, then every request at once (capacity)
     stream = [S.from_cluster(c) for _, c in W.config4_requests()]
-    srv = S.Server(eam, precision=fly.MIXED, hbm_budget_bytes=40 << 30, max_active=2048,
-                   steps_per_tick=args.steps_per_tick, tuning=out["config3"]["mixed"] and S.Tuning(
-                       **out["config3"]["mixed"]["tuning"]), dimer=opt)
-    rng = np.random.default_rng(1)
-    arrivals = np.cumsum(rng.exponential(1.0 / args.arrival_rate, len(stream)))
-    done: list = []
-    stop = threading.Event()
-
-    def poller():
-        while len(done) < len(stream) and not (stop.is_set() and len(done) >= len(stream)):
-            done.extend(srv.poll(512, wait_ms=20))
-            if stop.is_set() and srv.stats()["pending"] == 0 and srv.stats()["active"] == 0 and len(done) >= len(stream):
-                break
-
-    th = threading.Thread(target=poller)
-    th.start()
-    t0 = time.perf_counter()
-    for k, r in enumerate(stream):
-        while time.perf_counter() - t0 < arrivals[k]:
-            pass
-        srv.submit(r)
-    stop.set()
-    th.join(timeout=600)
-    elapsed = time.perf_counter() - t0
-    st = srv.stats()
-    srv.close()
-    lat = np.array([d["latency_ms"] for d in done])
-    ex = [d["exit_code"] for d in done]
-    out["config4"] = {"requests": len(stream), "completed": len(done), "arrival_rate_per_s": args.arrival_rate,
-                      "searches_per_s": len(done) / elapsed, "p50_ms": float(np.percentile(lat, 50)),
-                      "p99_ms": float(np.percentile(lat, 99)), "steps_per_tick": args.steps_per_tick,
-                      "ticks": st["ticks"], "converged": ex.count(0), "hbm_budget_bytes": 40 << 30,
-                      "plain_service_p50_ms": out["config3"]["plain_one_at_a_time"]["p50_ms"],
-                      "plain_service_p99_ms": out["config3"]["plain_one_at_a_time"]["p99_ms"]}
+    tune = S.Tuning(**out["config3"]["mixed"]["tuning"])
+    out["config4"] = serve_run(S, eam, stream, tune, opt, args, args.arrival_rate)
+    out["config4"]["plain_service_p50_ms"] = out["config3"]["plain_one_at_a_time"]["p50_ms"]
+    out["config4"]["plain_service_p99_ms"] = out["config3"]["plain_one_at_a_time"]["p99_ms"]
+    out["config4"]["saturated"] = serve_run(S, eam, stream, tune, opt, args, None)
     out["gpu_launches"] = int(fly.launch_count() - l0)
     return out
 
