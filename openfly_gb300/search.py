@@ -295,23 +295,53 @@ class Server:
         return {k: getattr(st, k) for k, _ in st._fields_}
 
 
-def pathways(eam: EAM, saddles: list[Search], minima: list[np.ndarray], precision: int = MIXED,
-             nudge_frac: float = 0.01, lbfgs: LBFGSOptions | None = None, tuning: Tuning | None = None):
-    """Master::do_adj_min (find.cpp:1014-1090) for many saddles at once: each saddle (positions = the
-    converged dimer, axis = its final axis) is nudged by +/- nudge_frac of its distance from the initial
-    minimum along the axis and both nudged states are relaxed with LBFGS::minimise, all in one batched
-    launch. As the reference, the relaxed state nearer the initial minimum is 'rev'. Returns one dict per
-    saddle: rev, fwd (n,3), E_rev, E_fwd, E_sp, barrier = E_sp - E_rev, and the minimisers' exit codes
-    (0 = converged). Clusters with frozen atoms need no translation freeze or drift correction; for a
-    fully mobile system the caller freezes one far atom first, as find.cpp:1026-1034 does."""
+def centroid(x: np.ndarray) -> np.ndarray:
+    """utility/lattice.hpp:203-209: the mean position."""
+    return np.asarray(x, np.float64).reshape(-1, 3).mean(axis=0)
+
+
+def centroid_align(x: np.ndarray, with_: np.ndarray) -> np.ndarray:
+    """utility/lattice.hpp:214-226: x translated so that its centroid is the centroid of ``with_``."""
+    x = np.asarray(x, np.float64).reshape(-1, 3)
+    return x + (centroid(with_) - centroid(x))
+
+
+def furthest_atom(pos: np.ndarray, extents, periodic, i: int) -> int:
+    """The entry for atom i of Master's separation list (find.cpp:224-243): the first atom at the largest
+    minimum-image distance from i."""
+    d = np.asarray(pos, np.float64).reshape(-1, 3) - np.asarray(pos, np.float64).reshape(-1, 3)[i]
+    for k in range(3):
+        if periodic[k]:
+            d[:, k] -= extents[k] * np.rint(d[:, k] / extents[k])
+    r = np.linalg.norm(d, axis=1)
+    return int(np.argmax(r)) if r.max() > 0 else 0  # argmax returns the first maximum, as the strict > loop
+
+
+def pathways(eam: EAM, saddles: list[Search], minima: list[np.ndarray], centres: list[int] | None = None,
+             precision: int = MIXED, nudge_frac: float = 0.01, lbfgs: LBFGSOptions | None = None,
+             tuning: Tuning | None = None):
+    """Master::do_adj_min (find.cpp:1014-1090) for many saddles at once, the relaxations in one batched
+    launch of the device minimiser. For each saddle (positions = the converged dimer, axis = its final
+    axis) both states nudged by +/- nudge_frac of its distance from the initial minimum along the axis
+    are relaxed with LBFGS::minimise; a system with no frozen atom has the atom furthest from its centre
+    frozen for the relaxations (find.cpp:1026-1034). Then, as the reference: no pathway (None) if a
+    relaxation fails; the relaxed state nearer the initial minimum is 'rev' (find.cpp:1054-1058); the
+    centre-of-mass drift of rev is removed from rev, the saddle and fwd (find.cpp:1062-1075); and, when
+    centres are given, no pathway unless the atom moving most between rev and fwd is the centre
+    (find.cpp:148-173, 1082-1087). Returns per saddle None or a dict: rev, sp, fwd (n,3), their energies
+    E_rev, E_sp, E_fwd (eV; translation leaves them unchanged), barrier = E_sp - E_rev, and the
+    minimisers' exit codes."""
     reqs = []
-    for s, x0 in zip(saddles, minima):
+    for k, (s, x0) in enumerate(zip(saddles, minima)):
         x = np.asarray(s.pos, np.float64).reshape(-1, 3)
         ax = np.asarray(s.axis, np.float64).reshape(-1, 3)
-        disp = np.linalg.norm(x - np.asarray(x0).reshape(-1, 3))
+        x0 = np.asarray(x0, np.float64).reshape(-1, 3)
+        disp = np.linalg.norm(x - x0)
+        fz = np.asarray(s.frozen, np.uint8).copy()
+        if int(fz.sum()) == 0 and centres is not None:
+            fz[furthest_atom(x0, s.extents, s.periodic, centres[k])] = 1
         for sign in (1.0, -1.0):
-            reqs.append(Search(x + sign * ax * disp * nudge_frac, s.types, s.frozen, s.extents, s.periodic,
-                               mode=MINIMISE))
+            reqs.append(Search(x + sign * ax * disp * nudge_frac, s.types, fz, s.extents, s.periodic, mode=MINIMISE))
     b = Batch(eam, reqs, precision=precision, lbfgs=lbfgs)
     b.run(tuning)
     res, pos, _ = b.results()
@@ -320,13 +350,23 @@ def pathways(eam: EAM, saddles: list[Search], minima: list[np.ndarray], precisio
     sp.run(tuning)
     e_sp = [r["energy"] for r in sp.results(positions=False)[0]]
     out = []
-    for k, x0 in enumerate(minima):
+    for k, (s, x0) in enumerate(zip(saddles, minima)):
         fwd, rev = pos[2 * k], pos[2 * k + 1]
         rf, rr = res[2 * k], res[2 * k + 1]
-        x0 = np.asarray(x0).reshape(-1, 3)
-        if np.linalg.norm(rev - x0) > np.linalg.norm(fwd - x0):  # find.cpp:1054-1058
+        if rf["status"] != 0 or rr["status"] != 0 or rf["exit_code"] != 0 or rr["exit_code"] != 0:
+            out.append(None)
+            continue
+        x0 = np.asarray(x0, np.float64).reshape(-1, 3)
+        if np.linalg.norm(rev - x0) > np.linalg.norm(fwd - x0):
             fwd, rev, rf, rr = rev, fwd, rr, rf
-        out.append(dict(rev=rev, fwd=fwd, E_rev=rr["energy"], E_fwd=rf["energy"], E_sp=e_sp[k],
+        drift = centroid(rev) - centroid(x0)
+        rev, x_sp, fwd = rev - drift, np.asarray(s.pos, np.float64).reshape(-1, 3) - drift, fwd - drift
+        if centres is not None:
+            r = ((rev - fwd) ** 2).sum(axis=1)
+            if (int(np.argmax(r)) if r.max() > 0 else 0) != centres[k]:
+                out.append(None)
+                continue
+        out.append(dict(rev=rev, sp=x_sp, fwd=fwd, E_rev=rr["energy"], E_sp=e_sp[k], E_fwd=rf["energy"],
                         barrier=e_sp[k] - rr["energy"], exit_rev=rr["exit_code"], exit_fwd=rf["exit_code"]))
     return out
 

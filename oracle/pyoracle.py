@@ -284,6 +284,58 @@ def lbfgs_minimise(data: EAMData, opt: LBFGSOptions, extents, periodic, pos, typ
     return bool(failed.value), iters.value, x.reshape(-1, 3), g.reshape(-1, 3)
 
 
+def furthest_atom(pos, extents, periodic, i: int) -> int:
+    """Master's separation list entry for atom i (saddle/find.cpp:224-243): the first atom at the largest
+    minimum-image distance from i."""
+    d = np.asarray(pos, np.float64) - np.asarray(pos, np.float64)[i]
+    for k in range(3):
+        if periodic[k]:
+            d[:, k] -= extents[k] * np.rint(d[:, k] / extents[k])
+    r = np.linalg.norm(d, axis=1)
+    k_best, best = 0, 0.0
+    for j in range(r.size):  # strict > keeps the first maximum, as the reference's loop
+        if r[j] > best:
+            k_best, best = j, r[j]
+    return k_best
+
+
+def adj_min(data: EAMData, opt: LBFGSOptions, extents, periodic, types, frozen, dimer_pos, dimer_axis, in_pos,
+            centre: int | None, nudge_frac: float = 0.01):
+    """Master::do_adj_min (saddle/find.cpp:1014-1090): relax from the saddle nudged by +/- nudge_frac of its
+    distance from the initial minimum along the axis (freezing the atom furthest from the centre when
+    nothing is frozen, :1026-1034), call the relaxed state nearer the initial minimum 'rev' (:1054-1058),
+    remove the centre-of-mass drift of rev from all three states (:1062-1075), and require the atom that
+    moves most between rev and fwd to be the centre (min_max, :148-173 and :1082-1087). Returns None
+    where the reference returns no pathway, else dict(rev, sp, fwd)."""
+    x0 = np.asarray(in_pos, np.float64).reshape(-1, 3)
+    x = np.asarray(dimer_pos, np.float64).reshape(-1, 3)
+    ax = np.asarray(dimer_axis, np.float64).reshape(-1, 3)
+    fz = np.asarray(frozen, np.uint8).copy()
+    disp = np.linalg.norm(x - x0)
+    if int(fz.sum()) == 0 and centre is not None:
+        fz[furthest_atom(x0, extents, periodic, centre)] = 1
+    got = []
+    for sign in (1.0, -1.0):
+        failed, _, xm, _ = lbfgs_minimise(data, opt, extents, periodic, x + sign * ax * disp * nudge_frac, types, fz)
+        if failed:
+            return None
+        got.append(xm)
+    fwd, rev = got
+    if np.linalg.norm(rev - x0) > np.linalg.norm(fwd - x0):
+        fwd, rev = rev, fwd
+    drift = rev.mean(axis=0) - x0.mean(axis=0)
+    rev, sp, fwd = rev - drift, x - drift, fwd - drift
+    if centre is not None:
+        r = ((rev - fwd) ** 2).sum(axis=1)
+        k_max, best = 0, 0.0
+        for j in range(r.size):
+            if r[j] > best:
+                k_max, best = j, r[j]
+        if k_max != centre:
+            return None
+    return dict(rev=rev, sp=sp, fwd=fwd)
+
+
 def dimer_find_sp(data: EAMData, opt: DimerOptions, extents, periodic, pos, axis, types, frozen, in_min=None,
                   hist=None, theta_tol: float = 0.0, count_frozen: int | None = None):
     """Dimer::find_sp. Returns dict(exit, steps, grad_calls, curv, x, axis)."""

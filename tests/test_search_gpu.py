@@ -180,34 +180,65 @@ def test_config1_periodic_search(gpu, oracle, odata, geam, search_mod):
             assert abs(r["energy"] - ref["energy"]) < E_TOL
 
 
+def _check_pathway(O, odata, s, p, ref, tag):
+    assert (p is None) == (ref is None), tag
+    if p is None:
+        return
+    for key in ("rev", "sp", "fwd"):
+        assert np.abs(p[key] - ref[key]).max() < SAME_SADDLE_A, (tag, key)
+    for key, e in (("rev", p["E_rev"]), ("fwd", p["E_fwd"])):
+        assert abs(e - oracle_energy(O, odata, s, ref[key])) < E_TOL, (tag, key)
+    assert abs(p["E_sp"] - oracle_energy(O, odata, s, ref["sp"])) < 1e-6, tag
+    assert p["barrier"] == p["E_sp"] - p["E_rev"]
+
+
 def test_pathways_match_oracle(gpu, oracle, odata, geam, search_mod, clusters):
-    # Master::do_adj_min (find.cpp:1014-1090): minima either side of converged saddles, vs the oracle's
-    # LBFGS::minimise from the same nudged starting points; saddle energy vs the oracle's EAM::energy.
+    # Master::do_adj_min (find.cpp:1014-1090) against the oracle's restatement: the two relaxations from
+    # the nudged saddle, the rev/fwd assignment, the centre-of-mass drift correction and the centre
+    # check (no pathway when the atom moving most is not the centre), on converged saddles.
     S, O = search_mod, oracle
     gopt, _ = c3_options(S, O)
     b = S.Batch(geam, [S.from_cluster(c) for c in clusters], precision=gpu.FP64, dimer=gopt)
     b.run(S.Tuning(4, 128, 2))
     res, pos, ax = b.results()
-    ok = [k for k, r in enumerate(res) if r["exit_code"] == 0][:5]
+    ok = [k for k, r in enumerate(res) if r["exit_code"] == 0][:6]
     assert ok
     sads = [S.Search(pos[k], clusters[k].sys.types, clusters[k].sys.frozen, clusters[k].sys.extents,
                      clusters[k].sys.periodic, axis=ax[k]) for k in ok]
     starts = [clusters[k].sys.pos for k in ok]
+    centres = [clusters[k].centre for k in ok]
     lopt = S.LBFGSOptions.defaults(f2norm=1e-4)
     olopt = O.LBFGSOptions.defaults(f2norm=1e-4)
-    paths = S.pathways(geam, sads, starts, precision=gpu.FP64, lbfgs=lopt)
-    for k, p in zip(ok, paths):
-        s = clusters[k].sys
-        assert abs(p["E_sp"] - oracle_energy(O, odata, s, pos[k])) < 1e-6
-        disp = np.linalg.norm(pos[k] - s.pos)
-        ref = []
-        for sign in (1.0, -1.0):
-            x = pos[k] + sign * ax[k] * disp * 0.01
-            failed, _, xm, _ = O.lbfgs_minimise(odata, olopt, s.extents, s.periodic, x, s.types, s.frozen)
-            ref.append(oracle_energy(O, odata, s, xm))
-        got = sorted([p["E_rev"], p["E_fwd"]])
-        assert max(abs(a - b_) for a, b_ in zip(got, sorted(ref))) < E_TOL
-        assert p["barrier"] == p["E_sp"] - p["E_rev"]
+    for cen in (None, centres):
+        paths = S.pathways(geam, sads, starts, centres=cen, precision=gpu.FP64, lbfgs=lopt)
+        for i, (k, p) in enumerate(zip(ok, paths)):
+            s = clusters[k].sys
+            ref = O.adj_min(odata, olopt, s.extents, s.periodic, s.types, s.frozen, pos[k], ax[k], s.pos,
+                            None if cen is None else cen[i])
+            _check_pathway(O, odata, s, p, ref, (k, cen is not None))
+
+
+def test_pathway_of_a_fully_mobile_cell(gpu, oracle, odata, geam, search_mod):
+    # No frozen atom: the relaxations freeze the atom furthest from the centre (find.cpp:1026-1034).
+    S, O = search_mod, oracle
+    s = W.config1()
+    centre = s.meta["centre"]
+    pos, axis = W.perturb(s, centre, np.random.default_rng(4))
+    gopt, _ = c3_options(S, O)
+    b = S.Batch(geam, [S.Search(pos, s.types, s.frozen, s.extents, s.periodic, axis=axis)], precision=gpu.FP64,
+                dimer=gopt)
+    b.run(S.Tuning(4, 256, 1))
+    res, sp, ax = b.results()
+    if res[0]["exit_code"] != 0:
+        pytest.skip("the config-1 search did not converge")
+    sad = S.Search(sp[0], s.types, s.frozen, s.extents, s.periodic, axis=ax[0])
+    lopt = S.LBFGSOptions.defaults(f2norm=1e-4)
+    olopt = O.LBFGSOptions.defaults(f2norm=1e-4)
+    p = S.pathways(geam, [sad], [s.pos], centres=[centre], precision=gpu.FP64, lbfgs=lopt)[0]
+    ref = O.adj_min(odata, olopt, s.extents, s.periodic, s.types, s.frozen, sp[0], ax[0], s.pos, centre)
+    assert S.furthest_atom(s.pos, s.extents, s.periodic, centre) == O.furthest_atom(s.pos, s.extents, s.periodic,
+                                                                                    centre)
+    _check_pathway(O, odata, s, p, ref, "config1")
 
 
 def test_minimise_matches_oracle(gpu, oracle, odata, geam, search_mod, clusters):
