@@ -101,10 +101,8 @@ namespace flygpu {
     o += up(sizeof(double) * static_cast<std::size_t>(n));
     l.need = o;
     o += up(sizeof(std::uint16_t) * static_cast<std::size_t>(n));
-    l.mnbr = o;
-    o += up(sizeof(std::uint16_t) * static_cast<std::size_t>(n) * NB_CAP);
-    l.mcnt = o;
-    o += up(sizeof(std::uint16_t) * static_cast<std::size_t>(n));
+    l.mark = o;
+    o += up(sizeof(int) * static_cast<std::size_t>(n));
     l.dacc = o;
     o += up(sizeof(long long) * static_cast<std::size_t>(n));
     l.total = o;
@@ -123,8 +121,7 @@ namespace flygpu {
     S.mob = reinterpret_cast<std::uint8_t*>(base + l.mob);
     S.rho0 = reinterpret_cast<double*>(base + l.rho0);
     S.need = reinterpret_cast<std::uint16_t*>(base + l.need);
-    S.mnbr = reinterpret_cast<std::uint16_t*>(base + l.mnbr);
-    S.mcnt = reinterpret_cast<std::uint16_t*>(base + l.mcnt);
+    S.mark = reinterpret_cast<int*>(base + l.mark);
     S.dacc = reinterpret_cast<long long*>(base + l.dacc);
   }
 

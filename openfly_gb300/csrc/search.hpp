@@ -78,8 +78,7 @@ namespace flygpu {
     std::uint8_t* mob;      // per atom: 1 if it can move (mobile), else 0
     double* rho0;           // per static atom: density from its static neighbours (fixed for the search)
     std::uint16_t* need;    // atoms whose F' the force pass reads (mobile atoms and their neighbours)
-    std::uint16_t* mnbr;    // [NB_CAP][n]: mobile neighbours of each needed static atom
-    std::uint16_t* mcnt;    // per atom: count in mnbr
+    int* mark;              // per atom: scratch flag of the needed-list build
     long long* dacc;        // per atom: its mobile neighbours' density terms in fixed point (L2 atomics)
     int n_need, pad2;
     double trust, acc, convex, curv, energy;
@@ -102,7 +101,7 @@ namespace flygpu {
 
   // Byte offsets of one search's arrays inside its block (256-byte aligned parts).
   struct SearchLayout {
-    std::size_t xl, pk, type, aatom, ncnt, nbr, vec, hist, mob, rho0, need, mnbr, mcnt, dacc, total;
+    std::size_t xl, pk, type, aatom, ncnt, nbr, vec, hist, mob, rho0, need, mark, dacc, total;
   };
 
   // search_{m,d}{1,2,4,8}.cu: the kernel variants of one precision and lanes-per-atom.

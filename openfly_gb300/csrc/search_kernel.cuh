@@ -96,8 +96,7 @@ namespace flygpu {
       std::uint8_t const* mob;
       double* rho0;
       std::uint16_t* need;
-      std::uint16_t* mnbr;
-      std::uint16_t* mcnt;
+      int* mark;
       long long* dacc;
       double rc2;
       float rc2f;
@@ -895,33 +894,21 @@ namespace flygpu {
       return sh.flag != 0;
     }
 
-    // Static atoms with a mobile neighbour ("needed": the force pass reads their F') and each one's
-    // mobile neighbours, in mobile-index order. The order of the needed list itself does not matter.
-    __device__ void static_lists(Ctx const& c, Blk& sh, double rc_list) {
-      float const lim = static_cast<float>((rc_list + 1e-3) * (rc_list + 1e-3));
+    // Static atoms with a mobile neighbour ("needed": the density pass scatters into them and the force
+    // pass reads their F'): the static entries of the mobile atoms' lists, which are exactly the static
+    // atoms that list a mobile atom (lists are symmetric). The order of the needed list does not matter.
+    __device__ void static_lists(Ctx const& c, Blk& sh, double) {
       if (threadIdx.x == 0) sh.n_need = 0;
+      for (int b = threadIdx.x; b < c.n; b += blockDim.x) c.mark[b] = 0;
       __syncthreads();
-      for (int b = threadIdx.x; b < c.n; b += blockDim.x) {
-        if (c.mob[b]) continue;
-        Packed const me = c.pk[b];
-        int mc = 0;
-        for (int k = 0; k < c.na; ++k) {
-          int const a = c.aatom[k];
-          Packed const o = c.pk[a];
-          float dx = o.hx - me.hx, dy = o.hy - me.hy, dz = o.hz - me.hz;
-          if (c.periodic) {
-            if (c.per[0]) dx -= c.Lf[0] * rintf(dx / c.Lf[0]);
-            if (c.per[1]) dy -= c.Lf[1] * rintf(dy / c.Lf[1]);
-            if (c.per[2]) dz -= c.Lf[2] * rintf(dz / c.Lf[2]);
-          }
-          if (dx * dx + dy * dy + dz * dz < lim) {
-            if (mc < NB_CAP) c.mnbr[static_cast<std::int64_t>(mc) * c.n + b] = static_cast<std::uint16_t>(a);
-            ++mc;
-          }
+      int const lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+      for (int k = threadIdx.x >> 5; k < c.na; k += nw) {
+        int const i = c.aatom[k];
+        int const cnt = c.ncnt[i];
+        for (int e = lane; e < cnt; e += 32) {
+          int const j = c.nbr[static_cast<std::int64_t>(e) * c.n + i];
+          if (!c.mob[j] && atomicCAS(&c.mark[j], 0, 1) == 0) c.need[atomicAdd(&sh.n_need, 1)] = static_cast<std::uint16_t>(j);
         }
-        if (mc > NB_CAP) atomicOr(&sh.flag, F_NLIST);
-        c.mcnt[b] = static_cast<std::uint16_t>(min(mc, NB_CAP));
-        if (mc > 0) c.need[atomicAdd(&sh.n_need, 1)] = static_cast<std::uint16_t>(b);
       }
       __syncthreads();
     }
@@ -1337,8 +1324,7 @@ namespace flygpu {
       cl.mob = S->mob;
       cl.rho0 = S->rho0;
       cl.need = S->need;
-      cl.mnbr = S->mnbr;
-      cl.mcnt = S->mcnt;
+      cl.mark = S->mark;
       cl.dacc = S->dacc;
       cl.rc2 = o.r_cut * o.r_cut;
       cl.rc2f = static_cast<float>(cl.rc2);
