@@ -434,6 +434,41 @@ def ours(args):
     h2d = 24 * n  # a displacement field, or the positions on rebuild steps
     d2h = 24 * n + 8
 
+    # the bit-exact binary64 path (the reference's arithmetic and summation order) on the same steps
+    def step64(j, sign, rb):
+        if rb:
+            nl.rebuild_device(d_pos_alt[j] if sign > 0 else d_pos0, n)
+        else:
+            nl.update_device(d_fields[j] if sign > 0 else d_neg[j])
+        eam.energy_gradient_device(nl, d_e, d_grad, precision=fly.FP64)
+
+    nl.rebuild_device(d_pos0, n)
+    for j, sign, rb in schedule(args.warmup):
+        step64(j, sign, rb)
+    sched64 = schedule(min(args.steps, 20))
+    torch.cuda.synchronize()
+    ev2, ev3 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev2.record(stream)
+    for j, sign, rb in sched64:
+        step64(j, sign, rb)
+    ev3.record(stream)
+    torch.cuda.synchronize()
+    ms64 = reduce_max(ev2.elapsed_time(ev3), dev)
+    fp64_line = {"value": replica_value(n, world, len(sched64), ms64), "unit": "atom-evals/s",
+                 "steps": len(sched64), "ms_per_step": ms64 / len(sched64),
+                 "note": "binary64 EAM in the reference's operation order (bit-identical to the oracle)"}
+
+    # catalogue local environments (geometry + fingerprint of every atom) from the same list
+    from openfly_gb300 import env as E
+
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    sizes = E.local_environments(nl, eam.r_cut(), s.types, s.frozen, copy=False)
+    env_s = time.perf_counter() - t0
+    env_line = {"atoms": n, "r_env_A": eam.r_cut(), "seconds": env_s, "atoms_per_s": n / env_s,
+                "r_ij_values": int(sizes["rij_values"]),
+                "note": "flygpu_env_build: every geometry and sorted fingerprint on the device (bit-exact binary64)"}
+
     # roofline of the dominant kernel
     peak, peak_kind = measured_peak_hbm()
     f_ms, f_cnt = ktimes["force"]
@@ -458,6 +493,8 @@ def ours(args):
         "step_algorithmic_GBps": ALGO_BYTES_STEP * n * args.steps / (ms * 1e-3) / 1e9,
         "gpu_launches": int(launches),
         "clocks": clk,
+        "fp64_exact": fp64_line,
+        "catalogue_envs": env_line,
     }
     if rank == 0 and not args.no_searches:
         line["searches"] = search_metrics(fly, args)

@@ -250,6 +250,29 @@ int flygpu_server_poll(flygpu_server* srv, int max, int wait_ms, flygpu_served* 
 int flygpu_server_take(flygpu_server* srv, uint64_t id, double* pos_out, double* axis_out);
 int flygpu_server_get_stats(flygpu_server* srv, flygpu_server_stats* stats);
 
+/* ------------------------------------------------------------------ catalogue local environments */
+
+typedef struct flygpu_env flygpu_env;
+
+/* The local environment of every atom of the list, as Catalogue::rebuild_env builds them before the
+ * graph hash (env/catalogue.cpp:66-78): the geometry of env/geometry.hpp:391-407 (rebuild_geo_from_nl:
+ * the atom at the origin, then its neighbours within r_env in the list's order, colour 2 type + frozen,
+ * shifted to the centroid) and the fingerprint of env/heuristics.hpp:93-110 (Fingerprint::rebuild:
+ * sorted distances to the central atom and between the others), binary64 in the reference's operation
+ * order. types (n entries, host) and frozen (n, host, 0/1) are by real-atom index; r_env <= the list's
+ * cut-off. The graph hash (canon_hash, nauty) is the caller's. */
+int flygpu_env_build(flygpu_list* list, double r_env, const uint32_t* types, const uint8_t* frozen,
+                     flygpu_env** out);
+/* Atoms, geometry entries (atoms + neighbours), r_0j values and r_ij values. */
+int flygpu_env_sizes(const flygpu_env* env, int64_t* n_atoms, int64_t* n_geo, int64_t* n_r0j, int64_t* n_rij);
+/* Host copies (each may be NULL): atom i's geometry is entries [geo_offsets[i], geo_offsets[i + 1]) of
+ * geo_pos (xyz), geo_colour and geo_index (real-atom index, the atom itself first); its r_0j values are
+ * [geo_offsets[i] - i, geo_offsets[i + 1] - i - 1) of r0j and its r_ij values [rij_offsets[i],
+ * rij_offsets[i + 1]) of rij, both ascending. Offsets have n + 1 entries. */
+int flygpu_env_get(const flygpu_env* env, int64_t* geo_offsets, double* geo_pos, int32_t* geo_colour,
+                   int32_t* geo_index, int64_t* rij_offsets, double* r0j, double* rij);
+void flygpu_env_destroy(flygpu_env* env);
+
 #ifdef __cplusplus
 }
 #endif

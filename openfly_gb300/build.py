@@ -19,7 +19,7 @@ LIB = os.path.join(OUT_DIR, "libflygpu.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off,-Wall"]
-EXACT = {"nlist.cu", "eam_fp64.cu", "noalloc.cu"}
+EXACT = {"nlist.cu", "eam_fp64.cu", "noalloc.cu", "env.cu"}
 
 
 def _nvcc() -> str:

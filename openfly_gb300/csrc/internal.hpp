@@ -250,6 +250,11 @@ namespace flygpu {
   // nlist.cu
   void list_rebuild(flygpu_list* L, double const* d_pos, std::int64_t n);
   void list_update(flygpu_list* L, double const* d_delta);
+  // For each real atom (reference index) its neighbours within r_cut in the list's order, on the device:
+  // offs[i] = first entry of atom i, idx (reference indices) and dr (xyz, binary64 r_n - r_i). Returns
+  // the per-atom counts on the host. Synchronises the list's stream.
+  std::vector<int> list_export_device(flygpu_list* L, double r_cut, DevBuf<long long>& offs, DevBuf<int>& idx,
+                                      DevBuf<double>& dr);
   // n_types bounds the type indices (out-of-range types raise FLYGPU_INVALID_ARG).
   void list_set_atoms(flygpu_list* L, int n_types, std::uint32_t const* d_types, std::uint8_t const* d_frozen,
                       bool copy_from_host, std::uint32_t const* h_types, std::uint8_t const* h_frozen);

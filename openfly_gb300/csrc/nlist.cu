@@ -616,4 +616,36 @@ namespace flygpu {
     return total;
   }
 
+  std::vector<int> list_export_device(flygpu_list* L, double r_cut, DevBuf<long long>& offs, DevBuf<int>& idx,
+                                      DevBuf<double>& dr) {
+    if (!L->built) fail(FLYGPU_INVALID_ARG, "neighbours() before rebuild()");
+    if (r_cut > L->g.rc) fail(FLYGPU_INVALID_ARG, "r_cut is bigger than the list's cut-off");
+    std::int64_t const n = L->n;
+    std::vector<int> hc(static_cast<std::size_t>(n));
+    if (n == 0) return hc;
+    cudaStream_t const s = L->stream;
+    double const rc2 = r_cut * r_cut;
+    DevBuf<int> d_counts;
+    d_counts.reserve(static_cast<std::size_t>(n));
+    launch(k_export_count, blocks_for(n), T, 0, s, L->pos.p, L->real_phys.p, L->pimg.p, L->nbr.p, L->ncount.p, n, rc2,
+           d_counts.p);
+    FLY_CUDA(cudaMemcpyAsync(hc.data(), d_counts.p, sizeof(int) * hc.size(), cudaMemcpyDeviceToHost, s));
+    FLY_CUDA(cudaStreamSynchronize(s));
+    std::vector<long long> ho(static_cast<std::size_t>(n));
+    long long total = 0;
+    for (std::int64_t i = 0; i < n; ++i) {
+      ho[static_cast<std::size_t>(i)] = total;
+      total += hc[static_cast<std::size_t>(i)];
+    }
+    offs.reserve(static_cast<std::size_t>(n));
+    idx.reserve(static_cast<std::size_t>(std::max<long long>(total, 1)));
+    dr.reserve(static_cast<std::size_t>(3 * std::max<long long>(total, 1)));
+    FLY_CUDA(cudaMemcpyAsync(offs.p, ho.data(), sizeof(long long) * ho.size(), cudaMemcpyHostToDevice, s));
+    if (total > 0)
+      launch(k_export_fill, blocks_for(n), T, 0, s, L->pos.p, L->real_phys.p, L->pimg.p, L->nbr.p, L->ncount.p, n, rc2,
+             offs.p, idx.p, dr.p);
+    FLY_CUDA(cudaStreamSynchronize(s));
+    return hc;
+  }
+
 }  // namespace flygpu

@@ -284,6 +284,30 @@ def lbfgs_minimise(data: EAMData, opt: LBFGSOptions, extents, periodic, pos, typ
     return bool(failed.value), iters.value, x.reshape(-1, 3), g.reshape(-1, 3)
 
 
+def local_environment(counts, idx, dr, types, frozen, i: int):
+    """Catalogue::rebuild_env up to the hash for atom i, from the list's (counts, idx, dr) in visiting
+    order: rebuild_geo_from_nl (env/geometry.hpp:391-407) and Fingerprint::rebuild (env/heuristics.hpp:
+    93-110), binary64 in the reference's operation order (sequential centroid sum, (x^2 + y^2) + z^2).
+    Returns (positions (K,3), colours, indices, sorted r_0j, sorted r_ij)."""
+    o = int(np.sum(counts[:i]))
+    c = int(counts[i])
+    p = [np.zeros(3)] + [np.asarray(dr[o + k], np.float64) for k in range(c)]
+    col = [2 * int(types[i]) + int(frozen[i])] + [2 * int(types[q]) + int(frozen[q]) for q in idx[o:o + c]]
+    ind = [i] + [int(q) for q in idx[o:o + c]]
+    s = np.zeros(3)
+    for v in p:  # Vec::Zero() += each position, in order
+        s = s + v
+    cen = s / float(len(p))
+    q = [v - cen for v in p]
+
+    def norm(d):
+        return np.sqrt((d[0] * d[0] + d[1] * d[1]) + d[2] * d[2])
+
+    r0 = sorted(norm(q[j] - q[0]) for j in range(1, len(q)))
+    rij = sorted(norm(q[a] - q[b]) for a in range(1, len(q)) for b in range(1, a))
+    return np.array(q), np.array(col), np.array(ind), np.array(r0), np.array(rij)
+
+
 def furthest_atom(pos, extents, periodic, i: int) -> int:
     """Master's separation list entry for atom i (saddle/find.cpp:224-243): the first atom at the largest
     minimum-image distance from i."""
