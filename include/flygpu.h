@@ -250,6 +250,15 @@ int flygpu_server_poll(flygpu_server* srv, int max, int wait_ms, flygpu_served* 
 int flygpu_server_take(flygpu_server* srv, uint64_t id, double* pos_out, double* axis_out);
 int flygpu_server_get_stats(flygpu_server* srv, flygpu_server_stats* stats);
 
+/* LBFGS::minimise (src/minimise/LBFGS/lbfgs.cpp:29-115) for one system of any size, every vector on the
+ * device: the whole-system relaxation an SKMC step ends with (kinetic/skmc.hpp:297-307). pos, types,
+ * frozen: host arrays (3n, n, n); pos_out (3n, may be NULL) receives the final positions. result:
+ * exit_code = LBFGS::minimise's bool (0 converged), steps, grad_calls, energy at the final positions.
+ * stream NULL: a private stream. */
+int flygpu_minimise(flygpu_eam* eam, const flygpu_lbfgs_options* lbfgs, int precision, int64_t n,
+                    const double* pos, const uint32_t* types, const uint8_t* frozen, const double extents[3],
+                    const int periodic[3], void* stream, double* pos_out, flygpu_search_result* result);
+
 /* ------------------------------------------------------------------ catalogue local environments */
 
 typedef struct flygpu_env flygpu_env;

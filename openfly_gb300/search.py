@@ -371,6 +371,29 @@ def pathways(eam: EAM, saddles: list[Search], minima: list[np.ndarray], centres:
     return out
 
 
+def minimise_system(eam: EAM, s: Search, precision: int = FP64, lbfgs: LBFGSOptions | None = None):
+    """LBFGS::minimise of one system of any size with every vector on the device (flygpu_minimise); returns
+    (result dict, final positions (n,3)). For a whole-system relaxation, not a batch of small ones."""
+    _setup()
+    L = lib()
+    if not getattr(L, "_minimise_ready", False):
+        V = C.c_void_p
+        L.flygpu_minimise.argtypes = [V, V, C.c_int, C.c_int64, V, V, V, V, V, V, V, V]
+        L._minimise_ready = True
+    pos = np.ascontiguousarray(s.pos, dtype=np.float64).reshape(-1)
+    ty = np.ascontiguousarray(s.types, dtype=np.uint32)
+    fz = np.ascontiguousarray(s.frozen, dtype=np.uint8)
+    ext = np.ascontiguousarray(s.extents, dtype=np.float64)
+    per = np.ascontiguousarray(s.periodic, dtype=np.int32)
+    out = np.zeros_like(pos)
+    r = SearchResult()
+    lbfgs = lbfgs or LBFGSOptions.defaults()
+    check(L.flygpu_minimise(eam.h, C.byref(lbfgs), precision, pos.size // 3, pos.ctypes.data, ty.ctypes.data,
+                            fz.ctypes.data, ext.ctypes.data, per.ctypes.data, None, out.ctypes.data, C.byref(r)),
+          "minimise_system")
+    return r.as_dict(), out.reshape(-1, 3)
+
+
 def search_plain(eam: EAM, s: Search, precision: int = FP64, dimer: DimerOptions | None = None,
                  lbfgs: LBFGSOptions | None = None):
     """One search the drop-in way; returns (result dict, positions (n,3), axis (n,3))."""
