@@ -1,0 +1,83 @@
+"""Host-side logic without a GPU: the synthetic workloads match the stated configurations, the bench's
+step schedule follows the reference's skin rule, and the pathway helpers agree with the oracle's
+restatements of Master's glue (find.cpp:148-243, utility/lattice.hpp:203-226)."""
+import numpy as np
+import pytest
+
+from openfly_gb300 import workloads as W
+
+
+def test_config2_sizes():
+    # 2 n^3 bcc sites, 0.1 % vacated, H = 0.05 % of the Fe count, periodic, sigma 0.05 A
+    s = W.config2(n_cells=12)
+    sites = 2 * 12 ** 3
+    n_vac = int(round(0.001 * sites))
+    n_fe = sites - n_vac
+    assert int((s.types == 0).sum()) == n_fe
+    assert int((s.types == 1).sum()) == int(round(0.0005 * n_fe))
+    assert s.periodic.tolist() == [1, 1, 1]
+    assert not s.frozen.any()
+    assert np.all((s.pos >= -1.0) & (s.pos <= s.extents + 1.0))
+
+
+def test_config3_clusters():
+    cl = W.config3(n=64, seed=3)
+    sizes = [c.sys.n for c in cl]
+    assert 50 <= min(sizes) and max(sizes) <= 520
+    for c in cl[:8]:
+        s = c.sys
+        assert s.periodic.tolist() == [0, 0, 0]
+        assert np.all(s.pos > 0) and np.all(s.pos < s.extents)  # enclosed with a margin
+        mobile = s.frozen == 0
+        assert mobile.any() and (~mobile).any()
+        assert np.isclose(np.linalg.norm(c.axis), 1.0)
+        assert not c.axis[~mobile].any()  # the axis lives on mobile atoms only
+
+
+def test_config4_stream():
+    reqs = W.config4_requests(n_env=6, seed=5)
+    envs = {e for e, _ in reqs}
+    assert len(envs) == 6
+    per = [sum(1 for e, _ in reqs if e == k) for k in envs]
+    assert min(per) >= 8 and max(per) <= 32
+    for _, c in reqs[:5]:
+        assert c.sys.frozen.any() and (c.sys.frozen == 0).any()
+
+
+def test_bench_schedule_follows_the_skin_rule():
+    import bench
+
+    sched = bench.schedule(100)
+    acc, rebuilds = 0.0, 0
+    for j, sign, rb in sched:
+        acc += bench.STEP_DISP
+        if acc > 0.5 * bench.SKIN:
+            assert rb
+            acc = 0.0
+            rebuilds += 1
+        else:
+            assert not rb
+    assert rebuilds == sum(1 for *_, rb in sched if rb) > 0
+    assert [sign for _, sign, _ in sched[:4]] == [1.0, -1.0, 1.0, -1.0]
+
+
+@pytest.mark.parametrize("seed", [1, 2])
+def test_furthest_atom_matches_oracle(oracle, seed):
+    from openfly_gb300 import search as S
+
+    rng = np.random.default_rng(seed)
+    ext = 5.0 + 10.0 * rng.random(3)
+    per = (rng.random(3) < 0.5).astype(np.int32)
+    pos = rng.random((200, 3)) * ext
+    for i in (0, 17, 199):
+        assert S.furthest_atom(pos, ext, per, i) == oracle.furthest_atom(pos, ext, per, i)
+
+
+def test_centroid_align():
+    from openfly_gb300 import search as S
+
+    rng = np.random.default_rng(7)
+    x, w = rng.normal(size=(50, 3)), rng.normal(size=(50, 3)) + 3.0
+    y = S.centroid_align(x, w)
+    assert np.allclose(S.centroid(y), S.centroid(w), atol=1e-12)
+    assert np.allclose(y - x, (S.centroid(w) - S.centroid(x))[None, :])
