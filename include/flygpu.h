@@ -114,6 +114,21 @@ int flygpu_eam_energy_gradient_device(flygpu_eam* eam, flygpu_list* list, const 
                                       const uint8_t* d_frozen, int precision, double* d_energy,
                                       double* d_grad);
 
+/* EAM::hessian (potential/EAM/eam.hpp:110, src/potential/EAM/eam.cpp:122-233): the dense 3n x 3n
+ * Hessian of the list's atoms in binary64, row-major, the rows 3a..3a+2 belonging to atom a. As in the
+ * reference only the lower 3x3 blocks (a >= z) are written, and the blocks of frozen atoms are zero;
+ * the values are the reference's, bit for bit. types (n) and frozen (n) are required; hess: 9 n^2
+ * doubles on the host. Neighbours are taken within the potential's cut-off from the list as built. */
+int flygpu_eam_hessian(flygpu_eam* eam, flygpu_list* list, const uint32_t* types, const uint8_t* frozen,
+                       double* hess);
+/* Hessian::mass_weight then Hessian::eigenvalues (system/hessian.hpp:86-93,136-143) of that Hessian,
+ * built, weighted and diagonalised on the device (the prefactor step of find.cpp:838-871 and
+ * Master::calc_minima_hess, find.cpp:1094-1144). masses: one per type (n_types doubles), NULL for the
+ * potential file's masses. eig: 3n doubles, ascending. hess (may be NULL): 9 n^2 doubles receiving the
+ * mass-weighted matrix. */
+int flygpu_hessian_eigenvalues(flygpu_eam* eam, flygpu_list* list, const uint32_t* types, const uint8_t* frozen,
+                               const double* masses, double* eig, double* hess);
+
 /* For callers that cannot allocate device memory (a host framework that owns every device allocation,
  * a real-time loop that must not touch the allocator after start-up, a caller holding only borrowed
  * device pointers). No reference counterpart. Computes the same energy and gradient as

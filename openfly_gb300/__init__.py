@@ -77,6 +77,8 @@ def lib() -> C.CDLL:
     L.flygpu_eam_gradient.argtypes = [V, V, V, V, C.c_int, V]
     L.flygpu_eam_energy_gradient.argtypes = [V, V, V, V, C.c_int, V, V]
     L.flygpu_eam_energy_gradient_device.argtypes = [V, V, V, V, C.c_int, V, V]
+    L.flygpu_eam_hessian.argtypes = [V, V, V, V, V]
+    L.flygpu_hessian_eigenvalues.argtypes = [V, V, V, V, V, V, V]
     _lib = L
     return L
 
@@ -166,6 +168,27 @@ class EAM:
         check(lib().flygpu_eam_energy_gradient(self.h, nl.h, _ptr(t), _ptr(f), precision, C.addressof(e), _ptr(g)),
               "EAM::energy+gradient")
         return e.value, g.reshape(-1, 3)
+
+    def hessian(self, types, frozen, nl: "List") -> np.ndarray:
+        """EAM::hessian (eam.hpp:110): the dense (3n, 3n) binary64 matrix, lower 3x3 blocks filled."""
+        n = nl.size()
+        h = np.zeros((3 * n, 3 * n), dtype=np.float64)
+        t, f = _host(types, np.uint32), _host(frozen, np.uint8)
+        check(lib().flygpu_eam_hessian(self.h, nl.h, t.ctypes.data, f.ctypes.data, h.ctypes.data), "EAM::hessian")
+        return h
+
+    def hessian_eigenvalues(self, types, frozen, nl: "List", masses=None, weighted: bool = False):
+        """Hessian::mass_weight + Hessian::eigenvalues (system/hessian.hpp:86-93,136-143) of EAM::hessian:
+        ascending eigenvalues (3n,); masses per type (None: the potential file's). With weighted=True
+        also returns the mass-weighted matrix."""
+        n = nl.size()
+        eig = np.zeros(3 * n, dtype=np.float64)
+        w = np.zeros((3 * n, 3 * n), dtype=np.float64) if weighted else None
+        t, f = _host(types, np.uint32), _host(frozen, np.uint8)
+        m = None if masses is None else _host(masses, np.float64)
+        check(lib().flygpu_hessian_eigenvalues(self.h, nl.h, t.ctypes.data, f.ctypes.data, _ptr(m), eig.ctypes.data,
+                                               _ptr(w)), "Hessian::eigenvalues")
+        return (eig, w) if weighted else eig
 
     def energy_gradient_device(self, nl: "List", d_energy, d_grad, d_types=None, d_frozen=None,
                                precision: int = MIXED) -> None:

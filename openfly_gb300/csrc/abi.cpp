@@ -305,6 +305,40 @@ int flygpu_eam_gradient(flygpu_eam* eam, flygpu_list* list, const uint32_t* type
   return flygpu_eam_energy_gradient(eam, list, types, frozen, precision, nullptr, grad);
 }
 
+int flygpu_eam_hessian(flygpu_eam* eam, flygpu_list* list, const uint32_t* types, const uint8_t* frozen, double* hess) {
+  return guard([&] {
+    need(eam && list && hess, "null argument");
+    need(list->built, "EAM call before List::rebuild()");
+    need(types && frozen, "types and frozen flags are required");
+    list_set_atoms(list, eam->n_types, nullptr, nullptr, true, types, frozen);
+    std::size_t const N = 3 * static_cast<std::size_t>(list->n);
+    DevBuf<double> H;
+    H.reserve(std::max<std::size_t>(N * N, 1));
+    eam_hessian(eam, list, H.p);
+    check_device(list);
+    if (N) FLY_CUDA(cudaMemcpy(hess, H.p, sizeof(double) * N * N, cudaMemcpyDeviceToHost));
+  });
+}
+
+int flygpu_hessian_eigenvalues(flygpu_eam* eam, flygpu_list* list, const uint32_t* types, const uint8_t* frozen,
+                               const double* masses, double* eig, double* hess) {
+  return guard([&] {
+    need(eam && list && eig, "null argument");
+    need(list->built, "EAM call before List::rebuild()");
+    need(types && frozen, "types and frozen flags are required");
+    list_set_atoms(list, eam->n_types, nullptr, nullptr, true, types, frozen);
+    std::size_t const N = 3 * static_cast<std::size_t>(list->n);
+    if (N == 0) return;
+    DevBuf<double> H;
+    H.reserve(N * N);
+    eam_hessian(eam, list, H.p);
+    check_device(list);
+    hessian_mass_weight(eam, list, masses, types, H.p);
+    if (hess) FLY_CUDA(cudaMemcpy(hess, H.p, sizeof(double) * N * N, cudaMemcpyDeviceToHost));
+    symmetric_eigenvalues(H.p, static_cast<std::int64_t>(N), list->stream, eig);
+  });
+}
+
 int flygpu_eam_energy_gradient_device(flygpu_eam* eam, flygpu_list* list, const uint32_t* d_types,
                                       const uint8_t* d_frozen, int precision, double* d_energy, double* d_grad) {
   return guard([&] {

@@ -274,6 +274,14 @@ namespace flygpu {
   void eam_fp64(flygpu_eam const* E, flygpu_list* L, double* d_energy, double* d_grad);
   void eam_mixed(flygpu_eam const* E, flygpu_list* L, double* d_energy, double* d_grad);
 
+  // hessian.cu: the dense 3n x 3n EAM Hessian into d_H (row-major, lower blocks); its mass weighting
+  // (type_mass per type, NULL for the potential file's masses); the ascending eigenvalues of a symmetric
+  // matrix given by its row-major lower triangle (d_H is overwritten). Each synchronises the stream.
+  void eam_hessian(flygpu_eam const* E, flygpu_list* L, double* d_H);
+  void hessian_mass_weight(flygpu_eam const* E, flygpu_list* L, double const* type_mass, std::uint32_t const* h_types,
+                           double* d_H);
+  void symmetric_eigenvalues(double* d_H, std::int64_t N, cudaStream_t s, double* h_eig);
+
   // tables.cpp
   void build_spline(std::vector<double> y, double dx, double* out4, int n_spines);
   int spline_spines(std::size_t n_samples);

@@ -452,6 +452,68 @@ namespace orc {
     }
   };
 
+  // EAM::hessian (src/potential/EAM/eam.cpp:122-233): the lower-triangular 3x3 blocks (a, z), a >= z,
+  // of the dense 3n x 3n Hessian into out (row-major; rows of atom a), everything else zero; a frozen
+  // atom's column and row blocks stay zero. Coefficients are formed in the order the reference's Eigen
+  // expressions evaluate them (outer products (s u_r) w_c, sums left to right).
+  inline void eam_hessian(EAM const& E, double* out, std::uint32_t const* t, std::uint8_t const* frozen, List const& nl,
+                          int threads) {
+    auto const& d = E.d;
+    long const n = nl.n, N = 3 * n;
+    std::fill(out, out + N * N, 0.0);
+    std::vector<double> rho(static_cast<std::size_t>(n)), mu(static_cast<std::size_t>(3 * n));
+    EAM::loop(n, threads, [&](long b) {  // rho and mu (A.13)
+      double rb = 0, m[3] = {0, 0, 0};
+      nl.for_neighbours(b, E.r_cut(), [&](long a, double r, double const* dr) {
+        rb += d->phi_of(t[a], t[b]).f(r);
+        double const fp = d->phi_of(t[a], t[b]).fp(r);
+        for (int k = 0; k < 3; ++k) m[k] -= fp * dr[k] / r;
+      });
+      rho[static_cast<std::size_t>(b)] = rb;
+      for (int k = 0; k < 3; ++k) mu[static_cast<std::size_t>(3 * b + k)] = m[k];
+    });
+    auto at = [&](long i, long j, int r, int c) -> double& { return out[(3 * i + r) * N + 3 * j + c]; };
+    EAM::loop(n, threads, [&](long z) {  // column block z only
+      if (frozen[z]) return;
+      double const* v = &mu[static_cast<std::size_t>(3 * z)];
+      double const fzpp = d->f_of(t[z]).fpp(rho[static_cast<std::size_t>(z)]);
+      for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) at(z, z, r, c) = (fzpp * v[r]) * v[c];
+      nl.for_neighbours(z, E.r_cut(), [&](long a, double r, double const* dr) {
+        double const rho_z = rho[static_cast<std::size_t>(z)], rho_a = rho[static_cast<std::size_t>(a)];
+        double const A = (d->v_of(t[a], t[z]).fp(r) + d->f_of(t[z]).fp(rho_z) * d->phi_of(t[a], t[z]).fp(r) +
+                          d->f_of(t[a]).fp(rho_a) * d->phi_of(t[z], t[a]).fp(r)) /
+                         r;
+        double const B = d->v_of(t[a], t[z]).fpp(r) + d->f_of(t[z]).fp(rho_z) * d->phi_of(t[a], t[z]).fpp(r) +
+                         d->f_of(t[a]).fp(rho_a) * d->phi_of(t[z], t[a]).fpp(r);
+        double const pza = d->phi_of(t[z], t[a]).fp(r);
+        double const ABFpp = (A - B - d->f_of(t[a]).fpp(rho_a) * (pza * pza)) / (r * r);
+        for (int i = 0; i < 3; ++i)
+          for (int c = 0; c < 3; ++c) at(z, z, i, c) += (i == c ? A : A * 0.0) - (ABFpp * dr[i]) * dr[c];
+        if (a > z && !frozen[a]) {
+          double const BArr = (B - A) / (r * r);
+          double const ur = d->f_of(t[z]).fpp(rho_z) * d->phi_of(t[a], t[z]).fp(r) / r;
+          double const ru = d->f_of(t[a]).fpp(rho_a) * d->phi_of(t[z], t[a]).fp(r) / r;
+          double const* muz = &mu[static_cast<std::size_t>(3 * z)];
+          double const* mua = &mu[static_cast<std::size_t>(3 * a)];
+          for (int i = 0; i < 3; ++i)
+            for (int c = 0; c < 3; ++c)
+              at(a, z, i, c) += (((-BArr * dr[i]) * dr[c] - (i == c ? A : A * 0.0)) + (ur * dr[i]) * muz[c]) -
+                                (ru * mua[i]) * dr[c];
+        }
+        double const ddFg = d->f_of(t[a]).fpp(rho_a) * d->phi_of(t[z], t[a]).fp(r);
+        nl.for_neighbours(a, E.r_cut(), [&](long g, double r_ag, double const* dr_ag) {
+          double const sx = dr[0] + dr_ag[0], sy = dr[1] + dr_ag[1], sz = dr[2] + dr_ag[2];
+          if ((g > z && !frozen[g]) || (g == z && std::sqrt((sx * sx + sy * sy) + sz * sz) > 1e-6)) {
+            double const mag = ddFg / (r * r_ag) * d->phi_of(t[g], t[a]).fp(r_ag);
+            for (int i = 0; i < 3; ++i)
+              for (int c = 0; c < 3; ++c) at(g, z, i, c) -= (mag * dr_ag[i]) * dr[c];
+          }
+        });
+      });
+    });
+  }
+
   // ---------------------------------------------------------------- vector helpers (core.hpp:634-680)
 
   using Vec = std::vector<double>;
@@ -943,6 +1005,14 @@ int orc_eam_gradient(void* h, void* l, std::uint32_t const* types, std::uint8_t 
   return guarded([&] {
     orc::EAM eam{static_cast<Handle*>(h)->data, {}};
     eam.gradient(g, types, frozen, *static_cast<orc::List*>(l), threads);
+  });
+}
+
+// EAM::hessian (eam.cpp:122-233) as a dense row-major 3n x 3n lower-block-triangular matrix.
+int orc_eam_hessian(void* h, void* l, std::uint32_t const* types, std::uint8_t const* frozen, int threads, double* out) {
+  return guarded([&] {
+    orc::EAM eam{static_cast<Handle*>(h)->data, {}};
+    orc::eam_hessian(eam, out, types, frozen, *static_cast<orc::List*>(l), threads);
   });
 }
 

@@ -113,6 +113,7 @@ def lib() -> C.CDLL:
         L.orc_list_raw.argtypes = [V, _ip, V, C.c_long]
         L.orc_eam_energy.argtypes = [V, V, _up, C.c_int, C.POINTER(C.c_double)]
         L.orc_eam_gradient.argtypes = [V, V, _up, _bp, C.c_int, _dp]
+        L.orc_eam_hessian.argtypes = [V, V, _up, _bp, C.c_int, _dp]
         L.orc_eam_fprime.argtypes = [V, V, _up, _bp, _dp]
         L.orc_brute_neighbours.restype = C.c_long
         L.orc_brute_neighbours.argtypes = [_dp, _ip, _dp, C.c_long, C.c_double, _ip, V, V, C.c_long]
@@ -249,6 +250,29 @@ def eam_gradient(data: EAMData, nl: List, types: np.ndarray, frozen: np.ndarray,
     _check(lib().orc_eam_gradient(data.h, nl.h, np.ascontiguousarray(types, dtype=np.uint32),
                                   np.ascontiguousarray(frozen, dtype=np.uint8), threads, g), "gradient")
     return g.reshape(-1, 3)
+
+
+def eam_hessian(data: EAMData, nl: List, types: np.ndarray, frozen: np.ndarray, threads: int = 1) -> np.ndarray:
+    """EAM::hessian (eam.cpp:122-233): the dense (3n, 3n) matrix with only its lower 3x3 blocks filled."""
+    h = np.zeros(9 * nl.n * nl.n, dtype=np.float64)
+    _check(lib().orc_eam_hessian(data.h, nl.h, np.ascontiguousarray(types, dtype=np.uint32),
+                                 np.ascontiguousarray(frozen, dtype=np.uint8), threads, h), "hessian")
+    return h.reshape(3 * nl.n, 3 * nl.n)
+
+
+def mass_weight(h: np.ndarray, masses: np.ndarray) -> np.ndarray:
+    """Hessian::mass_weight (system/hessian.hpp:136-143): every 3x3 block (j, i) times 1/sqrt(m_i m_j);
+    masses per atom."""
+    m = np.repeat(np.asarray(masses, np.float64), 3)
+    return h * (1.0 / np.sqrt(np.outer(m, m)))
+
+
+def hessian_eigenvalues(lower: np.ndarray, masses: np.ndarray | None = None) -> np.ndarray:
+    """Hessian::mass_weight (when masses are given) then Hessian::eigenvalues (system/hessian.hpp:86-93):
+    the ascending eigenvalues of the symmetric matrix the lower triangle defines (SelfAdjointEigenSolver
+    reads the lower triangle only)."""
+    w = lower if masses is None else mass_weight(lower, masses)
+    return np.linalg.eigvalsh(w, UPLO="L")
 
 
 def eam_fprime(data: EAMData, nl: List, types: np.ndarray, frozen: np.ndarray) -> np.ndarray:

@@ -1,0 +1,105 @@
+"""GPU EAM Hessian, mass weighting and eigenvalues through the C ABI, against the reference's known
+answers and the oracle. The Hessian and the mass-weighted matrix are bit-exact; the eigenvalues come
+from a different symmetric eigensolver than the oracle's and agree within EIG_TOL of the spectral
+radius."""
+import numpy as np
+import pytest
+
+from openfly_gb300 import workloads as W
+
+from test_hessian import KAT_H00, near
+
+pytestmark = pytest.mark.gpu
+
+EIG_TOL = 1e-10  # |lambda_gpu - lambda_oracle| <= EIG_TOL * max |lambda|
+
+
+def _pair(gpu, oracle, odata, s, rc):
+    g = gpu.List(s.extents, s.periodic, rc)
+    g.rebuild(s.pos)
+    o = oracle.List(s.extents, s.periodic, rc)
+    o.rebuild(s.pos, 1)
+    return g, o
+
+
+def _masses(odata, types):
+    return np.array([odata.mass(int(t)) for t in types])
+
+
+def test_kat_block_away_from_minimum(gpu, geam):
+    # tests/potential/EAM/eam.cpp:98-146
+    s = W.kat_lattice()
+    g = gpu.List(s.extents, s.periodic, geam.r_cut())
+    g.rebuild(s.pos)
+    h = geam.hessian(s.types, s.frozen, g)
+    assert np.linalg.norm(h[:3, :3] - KAT_H00) < 1e-10
+
+
+def test_kat_zero_modes_at_minimum(gpu, geam):
+    # tests/potential/EAM/eam.cpp:148-188 (unweighted: unit masses)
+    s = W.kat_lattice(erase=False)
+    g = gpu.List(s.extents, s.periodic, geam.r_cut())
+    g.rebuild(s.pos)
+    ev = geam.hessian_eigenvalues(s.types, s.frozen, g, masses=np.ones(geam.n_types))
+    assert all(near(e, 0.0) for e in ev[:3])
+    assert not any(near(e, 0.0) for e in ev[3:])
+
+
+def _systems():
+    rng = np.random.default_rng(21)
+    tight = W.bcc_sites(2, 2, 2, W.A_FE) + rng.normal(0, 0.05, (16, 3))
+    L = 2 * W.A_FE
+    return [
+        ("cluster", W.cluster(np.random.default_rng(3), 9.0, n_vac=1, n_h=2).sys, 0.0),
+        ("config1", W.config1(), 0.3),
+        ("tight", W.System(tight, np.zeros(16, np.uint32), np.zeros(16, np.uint8), np.full(3, L),
+                           np.ones(3, np.int32), {}), 0.0),
+    ]
+
+
+@pytest.mark.parametrize("name,s,skin", _systems(), ids=lambda v: v if isinstance(v, str) else "")
+def test_hessian_bit_exact_vs_oracle(gpu, oracle, geam, odata, name, s, skin):
+    # periodic images of an atom inside its own cut-off (the "tight" 2x2x2 cell) exercise the
+    # self-image overlap term and repeated neighbours g of one atom a
+    g, o = _pair(gpu, oracle, odata, s, odata.r_cut + skin)
+    h = geam.hessian(s.types, s.frozen, g)
+    ref = oracle.eam_hessian(odata, o, s.types, s.frozen, threads=4)
+    assert np.array_equal(h, ref), np.abs(h - ref).max()
+
+
+@pytest.mark.parametrize("name,s,skin", _systems(), ids=lambda v: v if isinstance(v, str) else "")
+def test_mass_weighted_eigenvalues_vs_oracle(gpu, oracle, geam, odata, name, s, skin):
+    g, o = _pair(gpu, oracle, odata, s, odata.r_cut + skin)
+    ev, w = geam.hessian_eigenvalues(s.types, s.frozen, g, weighted=True)
+    ref_h = oracle.eam_hessian(odata, o, s.types, s.frozen, threads=4)
+    m = _masses(odata, s.types)
+    assert np.array_equal(w, oracle.mass_weight(ref_h, m))
+    ref = oracle.hessian_eigenvalues(ref_h, m)
+    assert np.all(np.diff(ev) >= 0)
+    assert np.abs(ev - ref).max() <= EIG_TOL * np.abs(ref).max()
+    # frozen atoms contribute 3 zero modes each (find.cpp:1103-1110)
+    n_frozen = int(s.frozen.sum())
+    if n_frozen:
+        tol = 1e-6  # Master::Options::hessian_eigen_zero_tol (saddle/find.hpp:163)
+        assert int((np.abs(ev) <= tol).sum()) >= 3 * n_frozen
+
+
+def test_explicit_masses(gpu, oracle, geam, odata):
+    s = W.cluster(np.random.default_rng(8), 8.0, n_h=1).sys
+    g, o = _pair(gpu, oracle, odata, s, odata.r_cut)
+    per_type = np.array([50.0, 2.0])
+    ev, w = geam.hessian_eigenvalues(s.types, s.frozen, g, masses=per_type, weighted=True)
+    ref_h = oracle.eam_hessian(odata, o, s.types, s.frozen)
+    assert np.array_equal(w, oracle.mass_weight(ref_h, per_type[s.types]))
+
+
+def test_spline_out_of_bounds_is_reported(gpu, geam):
+    pos = np.full((200, 3), 5.0) + np.random.default_rng(0).normal(0, 1e-3, (200, 3))
+    g = gpu.List([10.0, 10.0, 10.0], [0, 0, 0], geam.r_cut())
+    g.rebuild(pos)
+    with pytest.raises(gpu.SplineOutOfBounds):
+        geam.hessian(np.zeros(200, np.uint32), np.zeros(200, np.uint8), g)
+    ok = np.array([[1.0, 1.0, 1.0], [3.5, 1.0, 1.0]])
+    g.rebuild(ok)
+    h = geam.hessian(np.zeros(2, np.uint32), np.zeros(2, np.uint8), g)
+    assert h.shape == (6, 6) and np.isfinite(h).all()
