@@ -481,6 +481,8 @@ def ours(args):
                 "ms_per_iteration": 1e3 * min_s / max(1, rmin["steps"]), "precision": "mixed", "history": lmin.n,
                 "note": "flygpu_minimise from the config-2 positions, list build and host transfers included"}
 
+    hess_line = hessian_prefactor(fly, eam)
+
     # roofline of the dominant kernel
     peak, peak_kind = measured_peak_hbm()
     f_ms, f_cnt = ktimes["force"]
@@ -508,6 +510,7 @@ def ours(args):
         "fp64_exact": fp64_line,
         "catalogue_envs": env_line,
         "minimise_system": min_line,
+        "hessian_prefactor": hess_line,
     }
     if rank == 0 and not args.no_searches:
         line["searches"] = search_metrics(fly, args)
@@ -525,11 +528,58 @@ def ours(args):
         _, it_cpu, _, _ = O.lbfgs_minimise(O.EAMData(W.TABLE), olmin, s.extents, s.periodic, s.pos, s.types, s.frozen)
         line["minimise_system"]["cpu_ms_per_iteration"] = 1e3 * (time.perf_counter() - t0) / max(1, it_cpu)
         line["minimise_system"]["cpu_sample"] = f"oracle LBFGS::minimise, {it_cpu} iterations, {threads} threads"
+        hs = HESS_SYSTEM()
+        od = O.EAMData(W.TABLE)
+        ol = O.List(hs.extents, hs.periodic, od.r_cut)
+        t0 = time.perf_counter()
+        ol.rebuild(hs.pos, 1)
+        hmat = O.eam_hessian(od, ol, hs.types, hs.frozen, threads=1)
+        t1 = time.perf_counter()
+        hm = [od.mass(int(t)) for t in hs.types]
+        O.hessian_eigenvalues(hmat, hm)
+        t2 = time.perf_counter()
+        act = np.repeat(hs.frozen == 0, 3)
+        O.hessian_eigenvalues(O.mass_weight(hmat, hm)[np.ix_(act, act)])
+        t3 = time.perf_counter()
+        line["hessian_prefactor"]["cpu_ms"] = {"hessian": 1e3 * (t1 - t0), "eigenvalues": 1e3 * (t2 - t1),
+                                               "eigenvalues_active_block": 1e3 * (t3 - t2)}
+        line["hessian_prefactor"]["cpu_sample"] = ("oracle EAM::hessian on 1 thread (the reference's call, find.cpp:840), "
+                                                   "then numpy eigvalsh (LAPACK, all host threads) of the full matrix "
+                                                   "and, separately, of the active block")
 
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist:
         tdist.destroy_process_group()
+
+
+def HESS_SYSTEM():
+    """The prefactor workload: a saddle-search sized cluster (vacancy + 2 H, frozen shell): 610 atoms, 114 mobile."""
+    from openfly_gb300 import workloads as W
+
+    return W.cluster(np.random.default_rng(77), 12.0, n_vac=1, n_h=2).sys
+
+
+def hessian_prefactor(fly, eam, reps: int = 5) -> dict:
+    """EAM::hessian + Hessian::mass_weight + Hessian::eigenvalues of one saddle-sized cluster through the
+    C ABI (list build, host copies and the eigensolve included), as Master's prefactor step runs them."""
+    hs = HESS_SYSTEM()
+    nl = fly.List(hs.extents, hs.periodic, eam.r_cut())
+    nl.rebuild(hs.pos)
+    eam.hessian_eigenvalues(hs.types, hs.frozen, nl)  # warm-up (solver handle, allocations)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        nl.rebuild(hs.pos)
+        ev = eam.hessian_eigenvalues(hs.types, hs.frozen, nl)
+    ms = 1e3 * (time.perf_counter() - t0) / reps
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        eam.hessian(hs.types, hs.frozen, nl)
+    ms_h = 1e3 * (time.perf_counter() - t0) / reps
+    tol = 1e-6
+    return {"atoms": hs.n, "frozen": int(hs.frozen.sum()), "matrix_dim": 3 * hs.n, "ms_per_system": ms,
+            "ms_hessian_to_host": ms_h, "zero_modes": int((np.abs(ev) <= tol).sum()),
+            "note": "flygpu_hessian_eigenvalues: binary64 Hessian (bit-exact), mass weighting, cuSOLVER syevd of the active block"}
 
 
 def search_batch(args) -> None:

@@ -335,7 +335,7 @@ int flygpu_hessian_eigenvalues(flygpu_eam* eam, flygpu_list* list, const uint32_
     check_device(list);
     hessian_mass_weight(eam, list, masses, types, H.p);
     if (hess) FLY_CUDA(cudaMemcpy(hess, H.p, sizeof(double) * N * N, cudaMemcpyDeviceToHost));
-    symmetric_eigenvalues(H.p, static_cast<std::int64_t>(N), list->stream, eig);
+    hessian_eigenvalues(list, H.p, frozen, eig);
   });
 }
 

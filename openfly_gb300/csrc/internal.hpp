@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -233,6 +234,8 @@ struct flygpu_list {
   bool packed_valid = false;
   // CUDA-event timing of the main kernels (enabled by flygpu_list_set_timing)
   bool timing = false;
+  std::shared_ptr<void> solver;  // cuSOLVER handle of the Hessian eigensolves (created on first use)
+  flygpu::DevBuf<double> solver_work;
   std::vector<cudaEvent_t> ev_pool;
   std::size_t ev_used = 0;
   struct Mark {
@@ -280,7 +283,11 @@ namespace flygpu {
   void eam_hessian(flygpu_eam const* E, flygpu_list* L, double* d_H);
   void hessian_mass_weight(flygpu_eam const* E, flygpu_list* L, double const* type_mass, std::uint32_t const* h_types,
                            double* d_H);
-  void symmetric_eigenvalues(double* d_H, std::int64_t N, cudaStream_t s, double* h_eig);
+  // The solver handle and workspace are the list's (L->solver, L->solver_work), on the list's stream.
+  void symmetric_eigenvalues(flygpu_list* L, double* d_H, std::int64_t N, double* h_eig);
+  // The same for a 3n x 3n Hessian whose frozen atoms' rows and columns are zero (only the active block
+  // is diagonalised; one exact zero per frozen coordinate is merged in).
+  void hessian_eigenvalues(flygpu_list* L, double* d_H, std::uint8_t const* h_frozen, double* h_eig);
 
   // tables.cpp
   void build_spline(std::vector<double> y, double dx, double* out4, int n_spines);
