@@ -67,6 +67,11 @@ int flygpu_eam_n_types(const flygpu_eam* eam);
 /* Host copy of one function's binary64 coefficients {a,b,c,d} per interval: kind 0 = F(type a),
  * 1 = phi(a, b), 2 = v(a, b). Returns the interval count; copies if cap >= 4 * count. */
 int64_t flygpu_eam_table(const flygpu_eam* eam, int kind, int a, int b, double* out, int64_t cap);
+/* Spline::Spline (src/utility/spline.cpp:27-103) on the host, the construction every EAM table goes
+ * through: the natural cubic spline of n >= 2 samples y spaced dx, padded with 5 copies of the last
+ * sample. Returns the interval count (n + 4); copies the binary64 {a,b,c,d} per interval if
+ * cap >= 4 * count. Needs no GPU. */
+int64_t flygpu_spline_build(const double* y, int64_t n, double dx, double* out, int64_t cap);
 
 /* ---------------------------------------------------------------- neighbour list
  * Replaces neigh::List::List(box, r_cut) (neigh/list.hpp:86-90) for an orthorhombic box

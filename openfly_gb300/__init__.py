@@ -78,9 +78,22 @@ def lib() -> C.CDLL:
     L.flygpu_eam_energy_gradient.argtypes = [V, V, V, V, C.c_int, V, V]
     L.flygpu_eam_energy_gradient_device.argtypes = [V, V, V, V, C.c_int, V, V]
     L.flygpu_eam_hessian.argtypes = [V, V, V, V, V]
+    L.flygpu_spline_build.restype = I64
+    L.flygpu_spline_build.argtypes = [V, I64, C.c_double, V, I64]
     L.flygpu_hessian_eigenvalues.argtypes = [V, V, V, V, V, V, V]
     _lib = L
     return L
+
+
+def spline_build(y, dx: float) -> np.ndarray:
+    """Spline::Spline (spline.cpp:27-103) as every EAM table is built: (n + 4, 4) binary64 {a,b,c,d}."""
+    y = np.ascontiguousarray(y, dtype=np.float64)
+    n = lib().flygpu_spline_build(y.ctypes.data, y.size, dx, None, 0)
+    if n < 0:
+        raise FlyGPUError(1, "Spline", lib().flygpu_last_error().decode())
+    out = np.zeros((n, 4), dtype=np.float64)
+    lib().flygpu_spline_build(y.ctypes.data, y.size, dx, out.ctypes.data, out.size)
+    return out
 
 
 def launch_count() -> int:

@@ -140,6 +140,19 @@ int64_t flygpu_eam_table(const flygpu_eam* eam, int kind, int a, int b, double* 
   return count;
 }
 
+int64_t flygpu_spline_build(const double* y, int64_t n, double dx, double* out, int64_t cap) {
+  if (!y || n < 2 || !(dx > 0)) {
+    set_error("spline needs at least two samples and a positive spacing");
+    return -1;
+  }
+  int const count = spline_spines(static_cast<std::size_t>(n));
+  if (out && cap >= 4 * static_cast<int64_t>(count)) {
+    int const st = guard([&] { build_spline(std::vector<double>(y, y + n), dx, out, count); });
+    if (st != FLYGPU_OK) return -1;
+  }
+  return count;
+}
+
 int flygpu_list_create(const double extents[3], const int periodic[3], double r_cut, void* stream, flygpu_list** out) {
   return guard([&] {
     need(extents && periodic && out, "null argument");

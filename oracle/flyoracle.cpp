@@ -916,6 +916,25 @@ long orc_spline_table(void* h, int kind, int a, int b, double* out, long cap) {
   return n;
 }
 
+// Spline::Spline (spline.cpp:27-103) of an arbitrary table: coefficients, and f / fp / fpp at points.
+long orc_spline_build(double const* y, long n, double dx, double* out, long cap) {
+  orc::Spline s(std::vector<double>(y, y + n), dx);
+  long const count = static_cast<long>(s.sp.size());
+  if (out && cap >= 4 * count) std::memcpy(out, s.sp.data(), sizeof(double) * 4 * static_cast<std::size_t>(count));
+  return count;
+}
+
+int orc_spline_points(double const* y, long n, double dx, double const* x, long m, double* out) {
+  return guarded([&] {
+    orc::Spline s(std::vector<double>(y, y + n), dx);
+    for (long k = 0; k < m; ++k) {
+      out[3 * k + 0] = s.f(x[k]);
+      out[3 * k + 1] = s.fp(x[k]);
+      out[3 * k + 2] = s.fpp(x[k]);
+    }
+  });
+}
+
 void* orc_list_new(double const* ext, int const* periodic, double r_cut) {
   try {
     return new orc::List(orc::Box(ext, periodic), r_cut);

@@ -114,6 +114,9 @@ def lib() -> C.CDLL:
         L.orc_eam_energy.argtypes = [V, V, _up, C.c_int, C.POINTER(C.c_double)]
         L.orc_eam_gradient.argtypes = [V, V, _up, _bp, C.c_int, _dp]
         L.orc_eam_hessian.argtypes = [V, V, _up, _bp, C.c_int, _dp]
+        L.orc_spline_build.restype = C.c_long
+        L.orc_spline_build.argtypes = [_dp, C.c_long, C.c_double, V, C.c_long]
+        L.orc_spline_points.argtypes = [_dp, C.c_long, C.c_double, _dp, C.c_long, _dp]
         L.orc_eam_fprime.argtypes = [V, V, _up, _bp, _dp]
         L.orc_brute_neighbours.restype = C.c_long
         L.orc_brute_neighbours.argtypes = [_dp, _ip, _dp, C.c_long, C.c_double, _ip, V, V, C.c_long]
@@ -258,6 +261,24 @@ def eam_hessian(data: EAMData, nl: List, types: np.ndarray, frozen: np.ndarray, 
     _check(lib().orc_eam_hessian(data.h, nl.h, np.ascontiguousarray(types, dtype=np.uint32),
                                  np.ascontiguousarray(frozen, dtype=np.uint8), threads, h), "hessian")
     return h.reshape(3 * nl.n, 3 * nl.n)
+
+
+def spline_build(y, dx: float) -> np.ndarray:
+    """Spline::Spline (spline.cpp:27-103): the (n + 4, 4) coefficients {a, b, c, d} of a sample table."""
+    y = np.ascontiguousarray(y, dtype=np.float64)
+    n = lib().orc_spline_build(y, y.size, dx, None, 0)
+    out = np.zeros((n, 4), dtype=np.float64)
+    lib().orc_spline_build(y, y.size, dx, out.ctypes.data, out.size)
+    return out
+
+
+def spline_points(y, dx: float, x) -> np.ndarray:
+    """Spline::f / fp / fpp (spline.hpp:100-123) of the spline of a sample table: (m, 3)."""
+    y = np.ascontiguousarray(y, dtype=np.float64)
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    out = np.zeros((x.size, 3), dtype=np.float64)
+    _check(lib().orc_spline_points(y, y.size, dx, x, x.size, out), "spline")
+    return out
 
 
 def mass_weight(h: np.ndarray, masses: np.ndarray) -> np.ndarray:

@@ -20,6 +20,16 @@ def _pair(gpu, oracle, geam, odata, s, rc_list):
     return g, o
 
 
+def test_tables_bit_exact_vs_oracle(gpu, geam, odata):
+    # DataEAM (data.cpp:67-153) + Spline (spline.cpp:27-103): every function's binary64 coefficients
+    nt = geam.n_types
+    for a in range(nt):
+        assert np.array_equal(geam.table(0, a), odata.table(0, a))
+        for b in range(nt):
+            assert np.array_equal(geam.table(1, a, b), odata.table(1, a, b))
+            assert np.array_equal(geam.table(2, a, b), odata.table(2, a, b))
+
+
 def test_kat_fp64(gpu, oracle, geam, odata):
     # tests/potential/EAM/eam.cpp:119,125
     s = W.kat_lattice()
