@@ -201,7 +201,10 @@ typedef struct {
 
 /* Launch shape of the batched search kernel: lanes per atom in the EAM passes (1, 2, 4, 8),
  * threads per CTA (multiple of 32), resident CTAs per SM of the persistent grid and the kernel
- * variant's register cap (0 = the compiler's allocation, 128 = at most 128 registers a thread). */
+ * variant's register cap (0 = the compiler's allocation, 128 = at most 128 registers a thread).
+ * Each CTA stages its search's vectors, positions and slot records in shared memory as far as its
+ * budget allows; the budget is the largest that keeps blocks_per_sm CTAs resident, so a higher
+ * residency trades staged state for more searches in flight. */
 typedef struct {
   int lanes_per_atom, threads, blocks_per_sm, max_registers;
 } flygpu_tuning;
@@ -221,7 +224,7 @@ int flygpu_batch_run(flygpu_batch* batch, const flygpu_tuning* tuning);
 int flygpu_batch_autotune(flygpu_batch* batch, flygpu_tuning* best);
 /* Restores every search's inputs so the batch can run again. */
 int flygpu_batch_reset(flygpu_batch* batch);
-/* Two-phase runs (the default: 100 steps, wide = {1, 256, 1, 0}): flygpu_batch_run first runs every
+/* Two-phase runs (the default: 100 steps, wide = {4, 512, 1, 128}): flygpu_batch_run first runs every
  * search for at most `steps` translation steps in the throughput shape, then the unfinished ones to
  * completion in the `wide` shape (one CTA per search with more threads: lower latency per step).
  * steps <= 0: one launch. wide NULL keeps the current wide shape. No reference counterpart (the

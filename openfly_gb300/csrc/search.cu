@@ -4,6 +4,8 @@
 
 #include <mutex>
 
+#include <algorithm>
+
 #include "search.hpp"
 
 namespace flygpu {
@@ -145,6 +147,20 @@ namespace flygpu {
     search_init_kernels();
     FLY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, pick(mixed, lanes_per_atom, max_registers),
                                                            threads, static_cast<std::size_t>(smem_bytes)));
+  }
+
+  int search_smem_for(int lanes_per_atom, int threads, bool mixed, int max_registers, int blocks_per_sm, int need) {
+    int bps = 0;
+    search_occupancy(lanes_per_atom, threads, mixed, max_registers, need, &bps);
+    if (bps >= blocks_per_sm) return need;
+    static int per_sm = 0;
+    if (!per_sm) FLY_CUDA(cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, 0));
+    // start from an even split of the SM's shared memory and step down by 1 KB
+    for (int b = std::min(need, per_sm / std::max(1, blocks_per_sm)) / 1024 * 1024; b >= 0; b -= 1024) {
+      search_occupancy(lanes_per_atom, threads, mixed, max_registers, b, &bps);
+      if (bps >= blocks_per_sm) return b;
+    }
+    return 0;
   }
 
   void search_launch(BatchView const& v, int lanes_per_atom, int threads, int max_registers, int blocks, bool mixed,

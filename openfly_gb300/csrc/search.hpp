@@ -125,6 +125,9 @@ namespace flygpu {
                      cudaStream_t s);
   void search_occupancy(int lanes_per_atom, int threads, bool mixed, int max_registers, int smem_bytes,
                         int* blocks_per_sm);
+  // The largest staging budget (dynamic shared memory per CTA, at most need) at which blocks_per_sm CTAs
+  // of the shape stay resident on one SM; 0 when even no staging does not allow that many.
+  int search_smem_for(int lanes_per_atom, int threads, bool mixed, int max_registers, int blocks_per_sm, int need);
   // Lets every kernel variant use SEARCH_SMEM_CAP bytes of dynamic shared memory (once per process;
   // call before any graph capture).
   void search_init_kernels();

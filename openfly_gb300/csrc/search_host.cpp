@@ -94,13 +94,13 @@ struct flygpu_batch {
   // Two-phase runs: the whole batch for straggler_steps translation steps with the throughput shape,
   // then the unfinished searches with the wide (low-latency) shape. straggler_steps <= 0: one phase.
   int straggler_steps = 100;
-  flygpu_tuning wide{1, 256, 1, 0};
+  flygpu_tuning wide{4, 512, 1, 128};
   DevBuf<int> order2, n2;
   bool tuned = false;
   flygpu_tuning tuning{};
   std::string tune_key;
 
-  BatchView view(int const* ord, int n_items, int budget, int const* n_items_dev = nullptr) {
+  BatchView view(int const* ord, int n_items, int budget, int const* n_items_dev = nullptr, int smem = -1) {
     BatchView v{};
     v.S = S.p;
     v.n_search = n_search;
@@ -109,7 +109,7 @@ struct flygpu_batch {
     v.n_items_dev = n_items_dev;
     v.work = work.p;
     v.budget = budget;
-    v.smem_bytes = smem_bytes;
+    v.smem_bytes = smem < 0 ? smem_bytes : smem;
     v.o = o;
     v.tb = eam->view();
     return v;
@@ -321,7 +321,7 @@ namespace flygpu {
     B->n2.reserve(1);
     FLY_CUDA(cudaStreamSynchronize(st));
     B->bytes = static_cast<std::int64_t>(B->S.n * sizeof(SearchDev) + 2 * off + 2 * B->out_x.n * 8);
-    // autotune cache key: device, precision and the size bucket of the batch
+    // autotune cache key: device, key version (r2: residency is tuned), precision and the size bucket
     double mean_n = static_cast<double>(atoms) / n_search, mean_a = static_cast<double>(act) / n_search;
     cudaDeviceProp prop{};
     int dev = 0;
@@ -330,7 +330,7 @@ namespace flygpu {
     std::ostringstream key;
     std::string name = prop.name;
     std::replace(name.begin(), name.end(), ' ', '_');
-    key << name << "/" << (B->mixed ? "mixed" : "fp64") << "/n" << (1 << static_cast<int>(std::lround(std::log2(std::max(1.0, mean_n)))))
+    key << name << "/r2/" << (B->mixed ? "mixed" : "fp64") << "/n" << (1 << static_cast<int>(std::lround(std::log2(std::max(1.0, mean_n)))))
         << "/a" << (1 << static_cast<int>(std::lround(std::log2(std::max(1.0, mean_a)))));
     B->tune_key = key.str();
   }
@@ -345,10 +345,14 @@ namespace flygpu {
   void batch_launch(flygpu_batch* B, flygpu_tuning const& t, int const* ord, int n_items, int budget,
                     int const* n_items_dev = nullptr) {
     if (t.threads % 32 || t.threads < 32 || t.threads > 1024) fail(FLYGPU_INVALID_ARG, "bad threads per CTA");
-    int const blocks = std::max(1, std::min(n_items, std::max(1, t.blocks_per_sm) * sm_count()));
+    int const bps = std::max(1, t.blocks_per_sm);
+    int const blocks = std::max(1, std::min(n_items, bps * sm_count()));
+    // staging budget: the batch's largest need, or less when that keeps more CTAs resident (a search
+    // stages as much of its state as fits and reads the rest from global memory)
+    int const smem = search_smem_for(t.lanes_per_atom, t.threads, B->mixed, t.max_registers, bps, B->smem_bytes);
     FLY_CUDA(cudaMemsetAsync(B->work.p, 0, sizeof(int), B->stream));
-    search_launch(B->view(ord, n_items, budget, n_items_dev), t.lanes_per_atom, t.threads, t.max_registers, blocks,
-                  B->mixed, B->stream);
+    search_launch(B->view(ord, n_items, budget, n_items_dev, smem), t.lanes_per_atom, t.threads, t.max_registers,
+                  blocks, B->mixed, B->stream);
   }
 
   // Every search of the batch to completion: one launch, or (straggler_steps > 0) a budgeted launch of
@@ -371,9 +375,10 @@ namespace flygpu {
       auto it = g_tune_cache.find(B->tune_key);
       if (it != g_tune_cache.end()) return it->second;
     }
-    // Sample: every k-th search of the size-sorted order, about two resident waves of the GPU.
+    // Sample: every k-th search of the size-sorted order, at least two resident waves of the GPU at the
+    // highest residency tried.
     int const sms = sm_count();
-    int const want = std::min(B->n_search, 4 * sms);
+    int const want = std::min(B->n_search, 12 * sms);
     std::vector<int> sample;
     for (int i = 0; i < want; ++i) sample.push_back(B->order[static_cast<std::size_t>(static_cast<std::int64_t>(i) * B->n_search / want)]);
     DevBuf<int> ord;
@@ -386,21 +391,27 @@ namespace flygpu {
     for (int lpa : {1, 2, 4, 8}) {
       for (int threads : {128, 256}) {
         for (int regs : {0, 128}) {
-          flygpu_tuning t{lpa, threads, 0, regs};
-          int bps = 0;
-          // resident CTAs per SM for this shape
-          search_occupancy(lpa, threads, B->mixed, regs, B->smem_bytes, &bps);
-          t.blocks_per_sm = std::max(1, bps);
-          batch_reset(B);
-          FLY_CUDA(cudaEventRecord(e0, B->stream));
-          batch_launch(B, t, ord.p, want, B->straggler_steps);  // the throughput phase
-          FLY_CUDA(cudaEventRecord(e1, B->stream));
-          FLY_CUDA(cudaEventSynchronize(e1));
-          float ms = 0;
-          FLY_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-          if (ms < best_ms) {
-            best_ms = ms;
-            best = t;
+          // resident CTAs per SM with the full staging budget, and with none (the register limit)
+          int full = 0, most = 0;
+          search_occupancy(lpa, threads, B->mixed, regs, B->smem_bytes, &full);
+          search_occupancy(lpa, threads, B->mixed, regs, 0, &most);
+          full = std::max(1, full);
+          std::vector<int> tries{full};
+          if (most > full + 1) tries.push_back((full + most) / 2);
+          if (most > full) tries.push_back(most);
+          for (int bps : tries) {
+            flygpu_tuning t{lpa, threads, bps, regs};
+            batch_reset(B);
+            FLY_CUDA(cudaEventRecord(e0, B->stream));
+            batch_launch(B, t, ord.p, want, B->straggler_steps);  // the throughput phase
+            FLY_CUDA(cudaEventRecord(e1, B->stream));
+            FLY_CUDA(cudaEventSynchronize(e1));
+            float ms = 0;
+            FLY_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+            if (ms < best_ms) {
+              best_ms = ms;
+              best = t;
+            }
           }
         }
       }
