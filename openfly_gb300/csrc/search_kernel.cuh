@@ -1014,15 +1014,158 @@ namespace flygpu {
       for (int e = threadIdx.x; e < c.M; e += 32) comp(c.xl[c.aatom[e / 3]], e % 3) -= sign * static_cast<double>(d[e]);
     }
 
+    // The same step with the direction q held in registers (K elements a lane, M <= 32 K): the two-loop
+    // recursion is a chain of 2m dependent warp reductions, and this form keeps every memory access off
+    // that chain. The next history pair is loaded while the current reduction runs. Each lane sums its
+    // elements in the memory form's order, so the results are the same.
+    template <bool MIXED, typename XT, int K>
+    __device__ __noinline__ void newton_reg(Ctx const& c, int m, int& k, double* s0, double* y0, double* rho, double* alpha,
+                               XT* px, Vt<MIXED>* pg, XT const* x, Vt<MIXED> const* g, Vt<MIXED>* out) {
+      using R = Red<MIXED>;
+      using V = Vt<MIXED>;
+      int const M = c.M;
+      int const lane = threadIdx.x;
+      auto S_ = [&](int j) { return vp<MIXED>(s0 + static_cast<std::int64_t>(j) * M); };
+      auto Y_ = [&](int j) { return vp<MIXED>(y0 + static_cast<std::int64_t>(j) * M); };
+      int const prev = k > 0 ? (k - 1) % m : 0;
+      V q[K];
+      if (k > 0) {
+        V* sp = S_(prev);
+        V* yp = Y_(prev);
+        R d = 0;
+#pragma unroll
+        for (int u = 0; u < K; ++u) {
+          int const e = lane + 32 * u;
+          if (e < M) {
+            V const sv = static_cast<V>(x[e] - px[e]);
+            V const yv = g[e] - pg[e];
+            sp[e] = sv;
+            yp[e] = yv;
+            d += static_cast<R>(sv) * static_cast<R>(yv);
+          }
+        }
+        R const ds = wsum<MIXED>(d);
+        double const r = scal<MIXED>([&] { return 1.f / fabsf(static_cast<float>(ds)); },
+                                     [&] { return 1.0 / fabs(ds); });
+        if (lane == 0) rho[prev] = r;
+      }
+#pragma unroll
+      for (int u = 0; u < K; ++u) {
+        int const e = lane + 32 * u;
+        q[u] = 0;
+        if (e < M) {
+          px[e] = x[e];
+          pg[e] = g[e];
+          q[u] = g[e];
+        }
+      }
+      __syncwarp();
+      int const incur = k <= m ? 0 : k - m;
+      int const bound = k <= m ? k : m;
+      auto load = [&](V const* p, V* r) {
+#pragma unroll
+        for (int u = 0; u < K; ++u) {
+          int const e = lane + 32 * u;
+          r[u] = e < M ? p[e] : V(0);
+        }
+      };
+      V sv[K], yv[K];
+      if (bound > 0) {
+        int const j = (bound - 1 + incur) % m;
+        load(S_(j), sv);
+        load(Y_(j), yv);
+      }
+      for (int i = bound - 1; i >= 0; --i) {
+        int const j = (i + incur) % m;
+        V sn[K], yn[K];
+        if (i > 0) {
+          int const jn = (i - 1 + incur) % m;
+          load(S_(jn), sn);
+          load(Y_(jn), yn);
+        }
+        R a = 0;
+#pragma unroll
+        for (int u = 0; u < K; ++u)
+          if (lane + 32 * u < M) a += static_cast<R>(sv[u]) * static_cast<R>(q[u]);
+        a = static_cast<R>(rho[j]) * wsum<MIXED>(a);
+        if (lane == 0) alpha[j] = a;
+        V const av = static_cast<V>(a);
+#pragma unroll
+        for (int u = 0; u < K; ++u) q[u] -= av * yv[u];
+        if (i > 0) {
+#pragma unroll
+          for (int u = 0; u < K; ++u) {
+            sv[u] = sn[u];
+            yv[u] = yn[u];
+          }
+        }
+      }
+      if (k > 0) {
+        V yl[K];
+        load(Y_(prev), yl);
+        R yy = 0;
+#pragma unroll
+        for (int u = 0; u < K; ++u)
+          if (lane + 32 * u < M) yy += static_cast<R>(yl[u]) * static_cast<R>(yl[u]);
+        yy = wsum<MIXED>(yy);
+        R const rp = static_cast<R>(rho[prev]);
+        V const scale = static_cast<V>(scal<MIXED>([&] { return 1.f / static_cast<float>(rp) / static_cast<float>(yy); },
+                                                   [&] { return 1.0 / rp / yy; }));
+#pragma unroll
+        for (int u = 0; u < K; ++u) q[u] = q[u] * scale;
+      }
+      __syncwarp();
+      if (bound > 0) {
+        int const j = incur % m;
+        load(S_(j), sv);
+        load(Y_(j), yv);
+      }
+      for (int i = 0; i <= bound - 1; ++i) {
+        int const j = (i + incur) % m;
+        V sn[K], yn[K];
+        if (i < bound - 1) {
+          int const jn = (i + 1 + incur) % m;
+          load(S_(jn), sn);
+          load(Y_(jn), yn);
+        }
+        R beta = 0;
+#pragma unroll
+        for (int u = 0; u < K; ++u)
+          if (lane + 32 * u < M) beta += static_cast<R>(yv[u]) * static_cast<R>(q[u]);
+        beta = static_cast<R>(rho[j]) * wsum<MIXED>(beta);
+        V const ab = static_cast<V>(static_cast<R>(alpha[j]) - beta);
+#pragma unroll
+        for (int u = 0; u < K; ++u) q[u] += ab * sv[u];
+        if (i < bound - 1) {
+#pragma unroll
+          for (int u = 0; u < K; ++u) {
+            sv[u] = sn[u];
+            yv[u] = yn[u];
+          }
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < K; ++u) {
+        int const e = lane + 32 * u;
+        if (e < M) out[e] = q[u];
+      }
+      __syncwarp();
+      ++k;
+    }
+
     // StepLBFGS::newton_step_impl (lbfgs_core.cpp:29-87), warp 0. History slot j of s (y) starts at
     // s0 + j M (y0 + j M) doubles and holds a V vector. x / px are positions (binary64) for the
-    // translation and the axis (V) for the rotation.
+    // translation and the axis (V) for the rotation. Up to 256 degrees of freedom the direction stays in
+    // registers (newton_reg); larger searches keep it in memory.
     template <bool MIXED, typename XT>
     __device__ void newton(Ctx const& c, int m, int& k, double* s0, double* y0, double* rho, double* alpha,
                            XT* px, Vt<MIXED>* pg, XT const* x, Vt<MIXED> const* g, Vt<MIXED>* out) {
       using R = Red<MIXED>;
       using V = Vt<MIXED>;
       int const M = c.M;
+      if (M <= 64) return newton_reg<MIXED, XT, 2>(c, m, k, s0, y0, rho, alpha, px, pg, x, g, out);
+      if (M <= 128) return newton_reg<MIXED, XT, 4>(c, m, k, s0, y0, rho, alpha, px, pg, x, g, out);
+      if (M <= 256) return newton_reg<MIXED, XT, 8>(c, m, k, s0, y0, rho, alpha, px, pg, x, g, out);
       int const lane = threadIdx.x;
       auto S_ = [&](int j) { return vp<MIXED>(s0 + static_cast<std::int64_t>(j) * M); };
       auto Y_ = [&](int j) { return vp<MIXED>(y0 + static_cast<std::int64_t>(j) * M); };
