@@ -608,6 +608,34 @@ def search_batch(args) -> None:
                       "errors": int(sum(r["status"] != 0 for r in res))}), flush=True)
 
 
+def search_tail(args) -> None:
+    """The tail of a config-3 batch as one launch, for profiling: the batch of --searches clusters runs
+    once (8 lanes, 256 threads, 2 CTAs/SM, 128-register variant, one phase); the searches that needed more
+    than 100 translation steps then run alone in the wide shape (4 lanes, 256 threads, 1 CTA/SM). Prints
+    one JSON line (not a bench line)."""
+    import openfly_gb300 as fly
+    from openfly_gb300 import search as S
+    from openfly_gb300 import workloads as W
+    from openfly_gb300.build import build
+
+    build()
+    eam = fly.EAM(W.TABLE)
+    opt = S.DimerOptions.defaults(n=6, rot_n=6, f2norm=1e-3, max_steps=1000)
+    cl = W.config3(n=args.searches, seed=7)
+    b = S.Batch(eam, [S.from_cluster(c) for c in cl], precision=fly.MIXED, dimer=opt)
+    b.set_stragglers(0)
+    b.run(S.Tuning(8, 256, 2, 128))
+    res, _, _ = b.results(positions=False)
+    tail = [k for k, r in enumerate(res) if r["steps"] > 100]
+    bt = S.Batch(eam, [S.from_cluster(cl[k]) for k in tail], precision=fly.MIXED, dimer=opt)
+    bt.set_stragglers(0)
+    t0 = time.perf_counter()
+    bt.run(S.Tuning(4, 256, 1, 0))
+    r2, _, _ = bt.results(positions=False)
+    print(json.dumps({"search_tail": len(tail), "seconds": time.perf_counter() - t0,
+                      "max_grad_calls": int(max(r["grad_calls"] for r in r2))}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--gpus", type=int, default=1)
@@ -626,9 +654,14 @@ def main():
                     help="only run one batch of this many config-3 searches (a small case for profilers)")
     ap.add_argument("--max-search-steps", type=int, default=1000, help="translation-step limit of --search-batch")
     ap.add_argument("--precision", choices=["mixed", "fp64"], default="mixed", help="precision of --search-batch")
+    ap.add_argument("--search-tail", action="store_true",
+                    help="only run the searches of a config-3 batch that outlast 100 steps, in one launch (profiling)")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")
+    if args.search_tail:
+        search_tail(args)
+        return
     if args.search_batch > 0:
         search_batch(args)
     elif args.impl == "reference":
