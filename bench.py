@@ -47,7 +47,7 @@ def log(*a):
 def make_workload(cells: int):
     from openfly_gb300 import workloads as W
 
-    s = W.config2(n_cells=cells)
+    s = W.fe_h_crystal(n_cells=cells)
     rng = np.random.default_rng(99)
     fields = []
     for _ in range(N_FIELDS):
@@ -137,9 +137,9 @@ def measured_peak_hbm() -> tuple[float, str]:
 
 def traffic_from_profile(kernel: str, atoms: int) -> float | None:
     """DRAM bytes (read + write) of one launch of `kernel` at `atoms` atoms, from the committed ncu
-    capture of a smaller case (profiles/eam_passes_config2.md), scaled by atom count: the traffic of a
+    capture of a smaller case (profiles/eam_passes_fe_h_crystal_split_records.md), scaled by atom count: the traffic of a
     pass grows in proportion to the atoms it processes."""
-    p = os.path.join(ROOT, "profiles", "c2_dram_traffic.json")
+    p = os.path.join(ROOT, "profiles", "fe_h_crystal_dram_traffic.json")
     if os.path.exists(p):
         k = json.load(open(p)).get(kernel)
         if k:
@@ -149,7 +149,7 @@ def traffic_from_profile(kernel: str, atoms: int) -> float | None:
 
 # ----------------------------------------------------------------------------- CPU (oracle) leg
 
-def cpu_c2(s, fields, steps: int, threads: int):
+def cpu_crystal_steps(s, fields, steps: int, threads: int):
     """The reference's CPU path (oracle port) on the same steps; returns (seconds, steps, rebuilds)."""
     from oracle import pyoracle as O
     from openfly_gb300 import workloads as W
@@ -183,8 +183,8 @@ def reference_arm(args):
     O.build()
     os.environ.setdefault("OMP_NUM_THREADS", str(threads))
     # warm-up then K timed steps, each a full step of the workload on every host thread
-    cpu_c2(s, fields, max(1, args.warmup), threads)
-    secs, k, rb = cpu_c2(s, fields, args.steps, threads)
+    cpu_crystal_steps(s, fields, max(1, args.warmup), threads)
+    secs, k, rb = cpu_crystal_steps(s, fields, args.steps, threads)
     value = s.n * k / secs
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "atom-evals/s", "n_gpus": args.gpus,
@@ -202,7 +202,7 @@ METRIC = "saddle searches/s + p50/p99 latency vs one-at-a-time GPU @<=1 meV; ato
 
 
 def config_dict(s, args, reference: bool = False):
-    c = {"workload": f"config 2: {args.cells}^3 bcc Fe, 0.1% vacancies, 0.05% H, sigma 0.05 A; per step "
+    c = {"workload": f"{args.cells}^3 bcc Fe, 0.1% vacancies, 0.05% H, sigma 0.05 A; per step "
                      f"List::update (skin {SKIN} A, rebuild by the reference's skin rule) + EAM energy+gradient",
          "atoms": s.n, "cells": args.cells}
     if reference:
@@ -218,7 +218,7 @@ def config_dict(s, args, reference: bool = False):
 # ----------------------------------------------------------------------------- search metrics
 
 def serve_run(S, eam, stream, tune, opt, args, rate) -> dict:
-    """Config 4 through flygpu_server: submit `stream` with Poisson arrivals at `rate` per second (all at
+    """The served stream through flygpu_server: submit `stream` with Poisson arrivals at `rate` per second (all at
     once when rate is None) and poll completions on another thread; searches/s over the wall time from
     the first submission to the last completion, latency from submission to completion."""
     import threading
@@ -268,9 +268,9 @@ def search_metrics(fly, args) -> dict:
 
     eam = fly.EAM(W.TABLE)
     opt = S.DimerOptions.defaults(n=6, rot_n=6, f2norm=1e-3, max_steps=1000)
-    clusters = W.config3(n=args.searches, seed=7)
+    clusters = W.search_clusters(n=args.searches, seed=7)
     reqs = [S.from_cluster(c) for c in clusters]
-    out = {"config3": {"searches": len(reqs), "mean_atoms": float(np.mean([r.n for r in reqs])),
+    out = {"batched": {"searches": len(reqs), "mean_atoms": float(np.mean([r.n for r in reqs])),
                        "options": "m=6 (translation and rotation), |F| < 1e-3 eV/A, <= 1000 steps"}}
     l0 = fly.launch_count()
     runs, pos_final = {}, {}
@@ -290,7 +290,7 @@ def search_metrics(fly, args) -> dict:
         runs[name] = res
         pos_final[name] = b.results(positions=True)[1]  # untimed: final configurations for the same-saddle test
         ex = [r["exit_code"] for r in res]
-        out["config3"][name] = {"searches_per_s": len(reqs) / best, "seconds": best, "tuning": tune.as_dict(),
+        out["batched"][name] = {"searches_per_s": len(reqs) / best, "seconds": best, "tuning": tune.as_dict(),
                                 "converged": ex.count(0), "convex": ex.count(-1), "iter_max": ex.count(-2),
                                 "errors": sum(r["status"] != 0 for r in res),
                                 "grad_calls_mean": float(np.mean([r["grad_calls"] for r in res]))}
@@ -300,7 +300,7 @@ def search_metrics(fly, args) -> dict:
             if a["exit_code"] == 0 and b_["exit_code"] == 0]
     same = [k for k in conv if np.abs(pos_final["mixed"][k] - pos_final["fp64"][k]).max() < SAME_SADDLE_A]
     err = np.abs(np.array([runs["mixed"][k]["energy"] - runs["fp64"][k]["energy"] for k in same])) * 1e3
-    out["config3"]["saddle_energy_err_mixed_vs_fp64_meV"] = {
+    out["batched"]["saddle_energy_err_mixed_vs_fp64_meV"] = {
         "n": int(err.size), "both_converged": len(conv), "same_saddle_A": SAME_SADDLE_A,
         "max": float(err.max()) if err.size else None,
         "p99": float(np.percentile(err, 99)) if err.size else None,
@@ -316,21 +316,21 @@ def search_metrics(fly, args) -> dict:
         S.search_plain(eam, r, fly.MIXED, dimer=opt)
         lat.append(1e3 * (time.perf_counter() - t1))
     plain = len(sample) / (time.perf_counter() - t0)
-    out["config3"]["plain_one_at_a_time"] = {"searches_per_s": plain, "sample": len(sample),
+    out["batched"]["plain_one_at_a_time"] = {"searches_per_s": plain, "sample": len(sample),
                                              "p50_ms": float(np.percentile(lat, 50)),
                                              "p99_ms": float(np.percentile(lat, 99))}
-    out["config3"]["batched_over_plain"] = out["config3"]["mixed"]["searches_per_s"] / plain
-    # served stream (config 4): Poisson arrivals at --arrival-rate, then every request at once (capacity)
-    stream = [S.from_cluster(c) for _, c in W.config4_requests()]
+    out["batched"]["batched_over_plain"] = out["batched"]["mixed"]["searches_per_s"] / plain
+    # served stream: Poisson arrivals at --arrival-rate, then every request at once (capacity)
+    stream = [S.from_cluster(c) for _, c in W.served_requests()]
     # served with the batch's lanes and threads at one CTA per SM and the compiler's register allocation:
     # the lowest latency per search (a served request waits on its own chain, not on the batch's tail)
-    t3 = out["config3"]["mixed"]["tuning"]
+    t3 = out["batched"]["mixed"]["tuning"]
     tune = S.Tuning(t3["lanes_per_atom"], t3["threads"], 1, 0)
-    out["config4"] = serve_run(S, eam, stream, tune, opt, args, args.arrival_rate)
-    out["config4"]["tuning"] = tune.as_dict()
-    out["config4"]["plain_service_p50_ms"] = out["config3"]["plain_one_at_a_time"]["p50_ms"]
-    out["config4"]["plain_service_p99_ms"] = out["config3"]["plain_one_at_a_time"]["p99_ms"]
-    out["config4"]["saturated"] = serve_run(S, eam, stream, tune, opt, args, None)
+    out["served"] = serve_run(S, eam, stream, tune, opt, args, args.arrival_rate)
+    out["served"]["tuning"] = tune.as_dict()
+    out["served"]["plain_service_p50_ms"] = out["batched"]["plain_one_at_a_time"]["p50_ms"]
+    out["served"]["plain_service_p99_ms"] = out["batched"]["plain_one_at_a_time"]["p99_ms"]
+    out["served"]["saturated"] = serve_run(S, eam, stream, tune, opt, args, None)
     out["gpu_launches"] = int(fly.launch_count() - l0)
     return out
 
@@ -483,7 +483,7 @@ def ours(args):
     min_s = time.perf_counter() - t0
     min_line = {"atoms": n, "iterations": rmin["steps"], "grad_calls": rmin["grad_calls"], "seconds": min_s,
                 "ms_per_iteration": 1e3 * min_s / max(1, rmin["steps"]), "precision": "mixed", "history": lmin.n,
-                "note": "flygpu_minimise from the config-2 positions, list build and host transfers included"}
+                "note": "flygpu_minimise from the crystal's positions, list build and host transfers included"}
 
     hess_line = hessian_prefactor(fly, eam)
 
@@ -521,7 +521,7 @@ def ours(args):
     if rank == 0 and not args.no_cpu and world == 1:
         threads = os.cpu_count() or 1
         os.environ.setdefault("OMP_NUM_THREADS", str(threads))
-        secs, k, rb = cpu_c2(s, fields, args.cpu_steps, threads)
+        secs, k, rb = cpu_crystal_steps(s, fields, args.cpu_steps, threads)
         line["cpu_baseline"] = {"value": n * k / secs, "unit": "atom-evals/s", "cores": threads, "kind": "port",
                                 "sample": f"{k} steps ({rb} rebuild) of the same {n}-atom workload, oracle port, "
                                           f"{threads} OpenMP threads"}
@@ -587,7 +587,7 @@ def hessian_prefactor(fly, eam, reps: int = 5) -> dict:
 
 
 def search_batch(args) -> None:
-    """One batched launch over --search-batch config-3 clusters (lanes 2, 128 threads, 2 CTAs/SM), for
+    """One batched launch over --search-batch search clusters (lanes 2, 128 threads, 2 CTAs/SM), for
     profiling the search kernel on a small case; prints one JSON line (not a bench line)."""
     import openfly_gb300 as fly
     from openfly_gb300 import search as S
@@ -598,7 +598,7 @@ def search_batch(args) -> None:
     eam = fly.EAM(W.TABLE)
     opt = S.DimerOptions.defaults(n=6, rot_n=6, f2norm=1e-3, max_steps=args.max_search_steps)
     prec = fly.MIXED if args.precision == "mixed" else fly.FP64
-    b = S.Batch(eam, [S.from_cluster(c) for c in W.config3(n=args.search_batch, seed=7)], precision=prec, dimer=opt)
+    b = S.Batch(eam, [S.from_cluster(c) for c in W.search_clusters(n=args.search_batch, seed=7)], precision=prec, dimer=opt)
     t0 = time.perf_counter()
     b.run(S.Tuning(2, 128, 2, 0))
     res, _, _ = b.results(positions=False)
@@ -609,7 +609,7 @@ def search_batch(args) -> None:
 
 
 def search_tail(args) -> None:
-    """The tail of a config-3 batch as one launch, for profiling: the batch of --searches clusters runs
+    """The tail of a batch of search clusters as one launch, for profiling: the batch of --searches clusters runs
     once (8 lanes, 256 threads, 2 CTAs/SM, 128-register variant, one phase); the searches that needed more
     than 100 translation steps then run alone in the wide shape (4 lanes, 256 threads, 1 CTA/SM). Prints
     one JSON line (not a bench line)."""
@@ -621,7 +621,7 @@ def search_tail(args) -> None:
     build()
     eam = fly.EAM(W.TABLE)
     opt = S.DimerOptions.defaults(n=6, rot_n=6, f2norm=1e-3, max_steps=1000)
-    cl = W.config3(n=args.searches, seed=7)
+    cl = W.search_clusters(n=args.searches, seed=7)
     b = S.Batch(eam, [S.from_cluster(c) for c in cl], precision=fly.MIXED, dimer=opt)
     b.set_stragglers(0)
     b.run(S.Tuning(8, 256, 2, 128))
@@ -651,11 +651,11 @@ def main():
     ap.add_argument("--arrival-rate", type=float, default=3000.0, help="served requests per second (Poisson)")
     ap.add_argument("--steps-per-tick", type=int, default=8, help="translation steps per serving tick")
     ap.add_argument("--search-batch", type=int, default=0,
-                    help="only run one batch of this many config-3 searches (a small case for profilers)")
+                    help="only run one batch of this many cluster searches (a small case for profilers)")
     ap.add_argument("--max-search-steps", type=int, default=1000, help="translation-step limit of --search-batch")
     ap.add_argument("--precision", choices=["mixed", "fp64"], default="mixed", help="precision of --search-batch")
     ap.add_argument("--search-tail", action="store_true",
-                    help="only run the searches of a config-3 batch that outlast 100 steps, in one launch (profiling)")
+                    help="only run the searches of a cluster batch that outlast 100 steps, in one launch (profiling)")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")

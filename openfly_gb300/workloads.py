@@ -63,7 +63,7 @@ def kat_lattice(erase: bool = True) -> System:
                   dict(a=a))
 
 
-def config1(seed: int = 1334) -> System:
+def fe_vacancy_cell(seed: int = 1334) -> System:
     """6x6x6 bcc Fe (432 sites, a = 2.855), one vacancy at the central site, seeded Gaussian noise
     sigma = 0.02 A, periodic. meta['centre'] is the vacancy's nearest neighbour the search centres on."""
     rng = np.random.default_rng(seed)
@@ -105,7 +105,7 @@ def perturb(sys: System, centre: int, rng: np.random.Generator, stddev: float = 
     return pos, axis
 
 
-def config2(n_cells: int = 80, seed: int = 2024) -> System:
+def fe_h_crystal(n_cells: int = 80, seed: int = 2024) -> System:
     """n_cells^3 bcc Fe (80^3 = 1,024,000 sites): 0.1 % of sites vacated at random, H equal to 0.05 %
     of the atom count on random distinct tetrahedral sites, seeded sigma = 0.05 A displacements,
     periodic. Atoms are returned in site order with the H appended."""
@@ -188,7 +188,7 @@ def cluster(rng: np.random.Generator, radius: float, shell: float = 5.5, n_vac: 
     return Cluster(s, axis, centre)
 
 
-def config4_box(seed: int = 16, cells: int = 20, n_vac: int = 5, n_h: int = 20) -> System:
+def served_box(seed: int = 16, cells: int = 20, n_vac: int = 5, n_h: int = 20) -> System:
     """The served workload's system: cells^3 bcc Fe (20^3 = 16,000 sites) with n_vac vacancies and n_h H
     on random distinct tetrahedral sites, seeded sigma = 0.02 A noise, periodic."""
     rng = np.random.default_rng(seed)
@@ -261,12 +261,12 @@ def cut_request(box: System, centre: int, radius: float, rng: np.random.Generato
     return Cluster(sub, axis, 0)
 
 
-def config4_requests(n_env: int = 96, seed: int = 44, r_min: float = 6.0, r_max: float = 11.0,
-                     per_env: tuple[int, int] = (8, 32)):
+def served_requests(n_env: int = 96, seed: int = 44, r_min: float = 6.0, r_max: float = 11.0,
+                    per_env: tuple[int, int] = (8, 32)):
     """The served request stream: n_env new local environments in the 16,000-site box, each emitting
     8-32 searches of clusters with radius ~ U(r_min, r_max). Returns a list of (environment, Cluster)."""
     rng = np.random.default_rng(seed)
-    box = config4_box()
+    box = served_box()
     out = []
     for e, c in enumerate(environment_centres(box, n_env, rng)):
         for _ in range(int(rng.integers(per_env[0], per_env[1] + 1))):
@@ -274,7 +274,7 @@ def config4_requests(n_env: int = 96, seed: int = 44, r_min: float = 6.0, r_max:
     return out
 
 
-def config3(n: int = 4096, seed: int = 7, r_min: float = 6.0, r_max: float = 11.0) -> list[Cluster]:
+def search_clusters(n: int = 4096, seed: int = 7, r_min: float = 6.0, r_max: float = 11.0) -> list[Cluster]:
     """n independent clusters with radii ~ U(r_min, r_max), 0-3 vacancies, 0-2 H (all seeded)."""
     rng = np.random.default_rng(seed)
     out = []

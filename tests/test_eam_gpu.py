@@ -42,7 +42,7 @@ def test_kat_fp64(gpu, oracle, geam, odata):
 
 
 def test_fp64_gradient_bit_exact_vs_oracle(gpu, oracle, geam, odata):
-    for s in (W.kat_lattice(), W.config1(), W.config2(n_cells=6)):
+    for s in (W.kat_lattice(), W.fe_vacancy_cell(), W.fe_h_crystal(n_cells=6)):
         g, o = _pair(gpu, oracle, geam, odata, s, odata.r_cut + 0.17)
         grad = geam.gradient(s.types, s.frozen, g, gpu.FP64)
         ref = oracle.eam_gradient(odata, o, s.types, s.frozen)
@@ -62,7 +62,7 @@ def test_frozen_atoms_have_zero_gradient(gpu, oracle, geam, odata):
 
 
 def test_update_then_gradient_bit_exact(gpu, oracle, geam, odata):
-    s = W.config1()
+    s = W.fe_vacancy_cell()
     g, o = _pair(gpu, oracle, geam, odata, s, odata.r_cut + 0.3)
     rng = np.random.default_rng(5)
     for _ in range(4):
@@ -73,7 +73,7 @@ def test_update_then_gradient_bit_exact(gpu, oracle, geam, odata):
 
 
 def test_mixed_within_stated_tolerance(gpu, oracle, geam, odata):
-    for s in (W.config1(), W.config2(n_cells=8)):
+    for s in (W.fe_vacancy_cell(), W.fe_h_crystal(n_cells=8)):
         g, o = _pair(gpu, oracle, geam, odata, s, odata.r_cut + 0.3)
         e, grad = geam.energy_gradient(s.types, s.frozen, g, gpu.MIXED)
         ref = oracle.eam_gradient(odata, o, s.types, s.frozen)

@@ -67,13 +67,13 @@ def _compare(gpu, oracle, s, r_env, update=None):
 @pytest.mark.gpu
 def test_gpu_environments_bit_exact(gpu, oracle, odata):
     # periodic cell with a vacancy, and a non-periodic cluster with a frozen shell and H (colours 0..3)
-    _compare(gpu, oracle, W.config1(), odata.r_cut)
+    _compare(gpu, oracle, W.fe_vacancy_cell(), odata.r_cut)
     cl = W.cluster(np.random.default_rng(8), 9.0, n_h=2, n_vac=1)
     _compare(gpu, oracle, cl.sys, 4.0)
 
 
 @pytest.mark.gpu
 def test_gpu_environments_after_update(gpu, oracle, odata):
-    s = W.config1()
+    s = W.fe_vacancy_cell()
     d = np.random.default_rng(2).normal(0.0, 0.02, s.pos.shape)
     _compare(gpu, oracle, s, odata.r_cut, update=d)

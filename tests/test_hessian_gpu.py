@@ -51,7 +51,7 @@ def _systems():
     L = 2 * W.A_FE
     return [
         ("cluster", W.cluster(np.random.default_rng(3), 9.0, n_vac=1, n_h=2).sys, 0.0),
-        ("config1", W.config1(), 0.3),
+        ("vacancy_cell", W.fe_vacancy_cell(), 0.3),
         ("tight", W.System(tight, np.zeros(16, np.uint32), np.zeros(16, np.uint8), np.full(3, L),
                            np.ones(3, np.int32), {}), 0.0),
     ]

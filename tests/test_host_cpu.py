@@ -7,9 +7,9 @@ import pytest
 from openfly_gb300 import workloads as W
 
 
-def test_config2_sizes():
+def test_fe_h_crystal_sizes():
     # 2 n^3 bcc sites, 0.1 % vacated, H = 0.05 % of the Fe count, periodic, sigma 0.05 A
-    s = W.config2(n_cells=12)
+    s = W.fe_h_crystal(n_cells=12)
     sites = 2 * 12 ** 3
     n_vac = int(round(0.001 * sites))
     n_fe = sites - n_vac
@@ -20,8 +20,8 @@ def test_config2_sizes():
     assert np.all((s.pos >= -1.0) & (s.pos <= s.extents + 1.0))
 
 
-def test_config3_clusters():
-    cl = W.config3(n=64, seed=3)
+def test_search_clusters():
+    cl = W.search_clusters(n=64, seed=3)
     sizes = [c.sys.n for c in cl]
     assert 50 <= min(sizes) and max(sizes) <= 520
     for c in cl[:8]:
@@ -34,8 +34,8 @@ def test_config3_clusters():
         assert not c.axis[~mobile].any()  # the axis lives on mobile atoms only
 
 
-def test_config4_stream():
-    reqs = W.config4_requests(n_env=6, seed=5)
+def test_served_requests():
+    reqs = W.served_requests(n_env=6, seed=5)
     envs = {e for e, _ in reqs}
     assert len(envs) == 6
     per = [sum(1 for e, _ in reqs if e == k) for k in envs]

@@ -23,9 +23,9 @@ def _energy(O, odata, s, x):
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_minimise_system_matches_oracle(gpu, oracle, odata, geam, S, precision):
-    # config 1 (431 atoms, periodic, a vacancy, sigma 0.02 A) relaxed to |F| < 1e-4 eV/A
+    # the 431-atom vacancy cell (periodic, sigma 0.02 A) relaxed to |F| < 1e-4 eV/A
     O = oracle
-    s = W.config1()
+    s = W.fe_vacancy_cell()
     prec = gpu.FP64 if precision == "fp64" else gpu.MIXED
     lopt = S.LBFGSOptions.defaults(f2norm=1e-4)
     olopt = O.LBFGSOptions.defaults(f2norm=1e-4)

@@ -64,8 +64,8 @@ def test_update_matches_oracle_exactly(gpu, oracle):
         assert np.array_equal(g.neighbours(rc)[0], cb)
 
 
-def test_config1_and_kat_cells(gpu, oracle, odata):
-    for s in (W.kat_lattice(), W.config1()):
+def test_vacancy_cell_and_kat_cells(gpu, oracle, odata):
+    for s in (W.kat_lattice(), W.fe_vacancy_cell()):
         rc = odata.r_cut + 0.3
         g = gpu.List(s.extents, s.periodic, rc)
         o = oracle.List(s.extents, s.periodic, rc)

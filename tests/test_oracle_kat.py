@@ -42,7 +42,7 @@ def test_eam_minimum_kat(oracle, odata):
 
 
 def test_threads_do_not_change_gradient(oracle, odata):
-    s = W.config1()
+    s = W.fe_vacancy_cell()
     nl = oracle.List(s.extents, s.periodic, odata.r_cut)
     nl.rebuild(s.pos, 4)
     g1 = oracle.eam_gradient(odata, nl, s.types, s.frozen, threads=1)

@@ -1,4 +1,4 @@
-"""bench.py's multi-GPU path is N independent replicas (searches and config-2 steps do not exchange data):
+"""bench.py's multi-GPU path is N independent replicas (searches and crystal steps do not exchange data):
 every rank runs the workload, timing is the maximum over ranks and the whole-job value counts all
 ranks' units. This runs that aggregation with two gloo ranks on the CPU (127.0.0.1)."""
 import os

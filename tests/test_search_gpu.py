@@ -26,7 +26,7 @@ def search_mod(gpu):
 
 @pytest.fixture(scope="module")
 def clusters():
-    return W.config3(n=32, seed=11)
+    return W.search_clusters(n=32, seed=11)
 
 
 @pytest.fixture(scope="module")
@@ -161,10 +161,10 @@ def test_plain_path_matches_oracle(gpu, oracle, odata, geam, search_mod, cluster
     compare(res, [p[1] for p in pick], "plain")
 
 
-def test_config1_periodic_search(gpu, oracle, odata, geam, search_mod):
+def test_vacancy_cell_periodic_search(gpu, oracle, odata, geam, search_mod):
     # 431-atom periodic cell, vacancy neighbour perturbed as Master::perturb does, f2norm 1e-3.
     S, O = search_mod, oracle
-    s = W.config1()
+    s = W.fe_vacancy_cell()
     pos, axis = W.perturb(s, s.meta["centre"], np.random.default_rng(4))
     gopt, oopt = c3_options(S, O)
     ref = O.dimer_find_sp(odata, oopt, s.extents, s.periodic, pos, axis, s.types, s.frozen)
@@ -221,7 +221,7 @@ def test_pathways_match_oracle(gpu, oracle, odata, geam, search_mod, clusters):
 def test_pathway_of_a_fully_mobile_cell(gpu, oracle, odata, geam, search_mod):
     # No frozen atom: the relaxations freeze the atom furthest from the centre (find.cpp:1026-1034).
     S, O = search_mod, oracle
-    s = W.config1()
+    s = W.fe_vacancy_cell()
     centre = s.meta["centre"]
     pos, axis = W.perturb(s, centre, np.random.default_rng(4))
     gopt, _ = c3_options(S, O)
@@ -230,7 +230,7 @@ def test_pathway_of_a_fully_mobile_cell(gpu, oracle, odata, geam, search_mod):
     b.run(S.Tuning(4, 256, 1))
     res, sp, ax = b.results()
     if res[0]["exit_code"] != 0:
-        pytest.skip("the config-1 search did not converge")
+        pytest.skip("the vacancy-cell search did not converge")
     sad = S.Search(sp[0], s.types, s.frozen, s.extents, s.periodic, axis=ax[0])
     lopt = S.LBFGSOptions.defaults(f2norm=1e-4)
     olopt = O.LBFGSOptions.defaults(f2norm=1e-4)
@@ -238,7 +238,7 @@ def test_pathway_of_a_fully_mobile_cell(gpu, oracle, odata, geam, search_mod):
     ref = O.adj_min(odata, olopt, s.extents, s.periodic, s.types, s.frozen, sp[0], ax[0], s.pos, centre)
     assert S.furthest_atom(s.pos, s.extents, s.periodic, centre) == O.furthest_atom(s.pos, s.extents, s.periodic,
                                                                                     centre)
-    _check_pathway(O, odata, s, p, ref, "config1")
+    _check_pathway(O, odata, s, p, ref, "vacancy_cell")
 
 
 def test_minimise_matches_oracle(gpu, oracle, odata, geam, search_mod, clusters):

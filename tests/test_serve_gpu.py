@@ -19,7 +19,7 @@ def S(gpu):
 
 @pytest.fixture(scope="module")
 def requests():
-    return [c for _, c in W.config4_requests(n_env=3, seed=5, per_env=(6, 8))]
+    return [c for _, c in W.served_requests(n_env=3, seed=5, per_env=(6, 8))]
 
 
 def alone(S, gpu, geam, cl, opt, tuning):

@@ -54,7 +54,7 @@ def allocating(gpu, geam, s):
 
 def test_noalloc_matches_allocating_entry_point(gpu, geam, noalloc):
     cl = W.cluster(np.random.default_rng(2), 9.5, n_vac=1, n_h=2)
-    systems = [W.config1(), W.kat_lattice(), cl.sys]
+    systems = [W.fe_vacancy_cell(), W.kat_lattice(), cl.sys]
     for s in systems + systems[:1]:  # consecutive calls reuse the shared scratch
         e, g = call(gpu, noalloc, geam, s)
         e_ref, g_ref = allocating(gpu, geam, s)
