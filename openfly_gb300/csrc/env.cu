@@ -186,11 +186,8 @@ namespace flygpu {
     E->rij.reserve(static_cast<std::size_t>(std::max<std::int64_t>(E->n_rij, 1)));
     launch(k_env_geo, static_cast<unsigned>((n + 127) / 128), 128, 0, s, n, offs1.p, idx.p, dr.p, ty.p, fz.p, E->pos.p,
            E->colour.p, E->index.p);
-    static bool attr = false;
-    if (!attr) {
-      FLY_CUDA(cudaFuncSetAttribute(k_env_fp, cudaFuncAttributeMaxDynamicSharedMemorySize, SORT_CAP * sizeof(double)));
-      attr = true;
-    }
+    // per call and on the current device (cheap; no shared state between host threads)
+    FLY_CUDA(cudaFuncSetAttribute(k_env_fp, cudaFuncAttributeMaxDynamicSharedMemorySize, SORT_CAP * sizeof(double)));
     int smax = 1;
     for (std::int64_t i = 0; i < n; ++i) {
       std::int64_t const c = cnt[static_cast<std::size_t>(i)];

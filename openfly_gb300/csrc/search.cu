@@ -153,8 +153,9 @@ namespace flygpu {
     int bps = 0;
     search_occupancy(lanes_per_atom, threads, mixed, max_registers, need, &bps);
     if (bps >= blocks_per_sm) return need;
-    static int per_sm = 0;
-    if (!per_sm) FLY_CUDA(cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, 0));
+    int dev = 0, per_sm = 0;
+    FLY_CUDA(cudaGetDevice(&dev));
+    FLY_CUDA(cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
     // start from an even split of the SM's shared memory and step down by 1 KB
     for (int b = std::min(need, per_sm / std::max(1, blocks_per_sm)) / 1024 * 1024; b >= 0; b -= 1024) {
       search_occupancy(lanes_per_atom, threads, mixed, max_registers, b, &bps);
