@@ -581,8 +581,25 @@ def hessian_prefactor(fly, eam, reps: int = 5) -> dict:
         eam.hessian(hs.types, hs.frozen, nl)
     ms_h = 1e3 * (time.perf_counter() - t0) / reps
     tol = 1e-6
+    # a batch of 32 search-sized clusters: one call on 8 worker streams, and the same systems one call each
+    from openfly_gb300 import search as S
+    from openfly_gb300 import workloads as W
+
+    systems = [S.from_cluster(c) for c in W.search_clusters(n=32, seed=77)]
+    S.hessian_eigenvalues_batch(eam, systems[:8])  # warm-up of the worker handles
+    t0 = time.perf_counter()
+    S.hessian_eigenvalues_batch(eam, systems, workers=8)
+    ms_b = 1e3 * (time.perf_counter() - t0) / len(systems)
+    t0 = time.perf_counter()
+    for x in systems:
+        nl1 = fly.List(x.extents, x.periodic, eam.r_cut())
+        nl1.rebuild(x.pos)
+        eam.hessian_eigenvalues(x.types, x.frozen, nl1)
+    ms_s = 1e3 * (time.perf_counter() - t0) / len(systems)
     return {"atoms": hs.n, "frozen": int(hs.frozen.sum()), "matrix_dim": 3 * hs.n, "ms_per_system": ms,
             "ms_hessian_to_host": ms_h, "zero_modes": int((np.abs(ev) <= tol).sum()),
+            "batch": {"systems": len(systems), "mean_atoms": float(np.mean([x.n for x in systems])), "workers": 8,
+                      "ms_per_system": ms_b, "one_call_each_ms_per_system": ms_s},
             "note": "flygpu_hessian_eigenvalues: binary64 Hessian (bit-exact), mass weighting, cuSOLVER syevd of the active block"}
 
 

@@ -282,6 +282,16 @@ int flygpu_minimise(flygpu_eam* eam, const flygpu_lbfgs_options* lbfgs, int prec
                     const double* pos, const uint32_t* types, const uint8_t* frozen, const double extents[3],
                     const int periodic[3], void* stream, double* pos_out, flygpu_search_result* result);
 
+/* The prefactor step for many systems in one call (the saddles, or minima, of one Master batch,
+ * find.cpp:838-871): for each system EAM::hessian, Hessian::mass_weight and Hessian::eigenvalues as
+ * flygpu_hessian_eigenvalues computes them, with each system's own list at the potential's cut-off.
+ * systems: n, pos, types, frozen, extents and periodic of each descriptor are read (the search fields are
+ * ignored). The systems run on `workers` host threads (<= 0: 8), each with its own stream, list and
+ * solver handle, so their latency-bound eigensolves overlap on the GPU. eig: the 3 n_k ascending
+ * eigenvalues of every system, concatenated in order. masses: per type, NULL for the file's. */
+int flygpu_hessian_eigenvalues_batch(flygpu_eam* eam, const flygpu_search_desc* systems, int n_systems,
+                                     const double* masses, int workers, double* eig);
+
 /* ------------------------------------------------------------------ catalogue local environments */
 
 typedef struct flygpu_env flygpu_env;

@@ -81,6 +81,7 @@ def lib() -> C.CDLL:
     L.flygpu_spline_build.restype = I64
     L.flygpu_spline_build.argtypes = [V, I64, C.c_double, V, I64]
     L.flygpu_hessian_eigenvalues.argtypes = [V, V, V, V, V, V, V]
+    L.flygpu_hessian_eigenvalues_batch.argtypes = [V, V, C.c_int, V, C.c_int, V]
     _lib = L
     return L
 

@@ -6,6 +6,8 @@
 #include <memory>
 #include <new>
 
+#include <thread>
+
 #include "internal.hpp"
 
 namespace flygpu {
@@ -79,6 +81,50 @@ namespace flygpu {
 
   void need(bool ok, char const* what) {
     if (!ok) fail(FLYGPU_INVALID_ARG, what);
+  }
+
+  // EAM::hessian + mass_weight + eigenvalues of the atoms of a built list (types / frozen already set;
+  // the host copies are read for the masses and the active block). hess (may be NULL) receives the
+  // mass-weighted matrix. Scratch stays in the list.
+  void hessian_prefactor_one(flygpu_eam* eam, flygpu_list* list, uint32_t const* types, uint8_t const* frozen,
+                             double const* masses, double* eig, double* hess) {
+    std::size_t const N = 3 * static_cast<std::size_t>(list->n);
+    if (N == 0) return;
+    DevBuf<double>& H = list->hs.H;
+    H.reserve(N * N);
+    eam_hessian(eam, list, H.p);
+    check_device(list);
+    hessian_mass_weight(eam, list, masses, types, H.p);
+    if (hess) {
+      FLY_CUDA(cudaMemcpyAsync(hess, H.p, sizeof(double) * N * N, cudaMemcpyDeviceToHost, list->stream));
+      FLY_CUDA(cudaStreamSynchronize(list->stream));
+    }
+    hessian_eigenvalues(list, H.p, frozen, eig);
+  }
+
+  // The box and cut-off of a list (neigh::List::List, neigh/list.hpp:86-90; HyperGrid, hypergrid.hpp:43-53):
+  // cell grid and the offset of the binary32 packed coordinates. The list must be rebuilt afterwards.
+  void list_set_box(flygpu_list* L, double const extents[3], int const periodic[3], double r_cut) {
+    need(r_cut > 0, "r_cut must be positive");
+    GridDesc g{};
+    g.rc = r_cut;
+    double shift[3];
+    for (int k = 0; k < 3; ++k) {
+      need(extents[k] > 0, "box extents must be positive");
+      need(extents[k] > r_cut, "r_cut is too big for the box");  // hypergrid.hpp:46-48
+      g.L[k] = extents[k];
+      g.per[k] = periodic[k] ? 1 : 0;
+      g.shape[k] = 2 + static_cast<int>(extents[k] / r_cut);
+      g.cell[k] = extents[k] / std::floor(extents[k] / r_cut);
+      g.inv_cell[k] = 1.0 / g.cell[k];
+      double const C = std::exp2(std::ceil(std::log2(extents[k] + 4 * r_cut + 1)));
+      shift[k] = C + 2 * r_cut;
+    }
+    need(static_cast<double>(g.shape[0]) * g.shape[1] * g.shape[2] < 2e9, "too many cells");
+    L->g = g;
+    for (int k = 0; k < 3; ++k) L->shift[k] = shift[k];
+    L->built = false;
+    L->packed_valid = false;
   }
 
   void run_eam(flygpu_eam* E, flygpu_list* L, int precision, double* d_energy, double* d_grad) {
@@ -157,22 +203,8 @@ int flygpu_list_create(const double extents[3], const int periodic[3], double r_
   return guard([&] {
     need(extents && periodic && out, "null argument");
     *out = nullptr;
-    need(r_cut > 0, "r_cut must be positive");
     auto L = std::make_unique<flygpu_list>();
-    GridDesc& g = L->g;
-    g.rc = r_cut;
-    for (int k = 0; k < 3; ++k) {
-      need(extents[k] > 0, "box extents must be positive");
-      need(extents[k] > r_cut, "r_cut is too big for the box");  // hypergrid.hpp:46-48
-      g.L[k] = extents[k];
-      g.per[k] = periodic[k] ? 1 : 0;
-      g.shape[k] = 2 + static_cast<int>(extents[k] / r_cut);
-      g.cell[k] = extents[k] / std::floor(extents[k] / r_cut);
-      g.inv_cell[k] = 1.0 / g.cell[k];
-      double const C = std::exp2(std::ceil(std::log2(extents[k] + 4 * r_cut + 1)));
-      L->shift[k] = C + 2 * r_cut;
-    }
-    need(static_cast<double>(g.shape[0]) * g.shape[1] * g.shape[2] < 2e9, "too many cells");
+    list_set_box(L.get(), extents, periodic, r_cut);
     if (stream) {
       L->stream = static_cast<cudaStream_t>(stream);
     } else {
@@ -325,11 +357,13 @@ int flygpu_eam_hessian(flygpu_eam* eam, flygpu_list* list, const uint32_t* types
     need(types && frozen, "types and frozen flags are required");
     list_set_atoms(list, eam->n_types, nullptr, nullptr, true, types, frozen);
     std::size_t const N = 3 * static_cast<std::size_t>(list->n);
-    DevBuf<double> H;
-    H.reserve(std::max<std::size_t>(N * N, 1));
+    if (N == 0) return;
+    DevBuf<double>& H = list->hs.H;
+    H.reserve(N * N);
     eam_hessian(eam, list, H.p);
     check_device(list);
-    if (N) FLY_CUDA(cudaMemcpy(hess, H.p, sizeof(double) * N * N, cudaMemcpyDeviceToHost));
+    FLY_CUDA(cudaMemcpyAsync(hess, H.p, sizeof(double) * N * N, cudaMemcpyDeviceToHost, list->stream));
+    FLY_CUDA(cudaStreamSynchronize(list->stream));
   });
 }
 
@@ -340,15 +374,72 @@ int flygpu_hessian_eigenvalues(flygpu_eam* eam, flygpu_list* list, const uint32_
     need(list->built, "EAM call before List::rebuild()");
     need(types && frozen, "types and frozen flags are required");
     list_set_atoms(list, eam->n_types, nullptr, nullptr, true, types, frozen);
-    std::size_t const N = 3 * static_cast<std::size_t>(list->n);
-    if (N == 0) return;
-    DevBuf<double> H;
-    H.reserve(N * N);
-    eam_hessian(eam, list, H.p);
-    check_device(list);
-    hessian_mass_weight(eam, list, masses, types, H.p);
-    if (hess) FLY_CUDA(cudaMemcpy(hess, H.p, sizeof(double) * N * N, cudaMemcpyDeviceToHost));
-    hessian_eigenvalues(list, H.p, frozen, eig);
+    hessian_prefactor_one(eam, list, types, frozen, masses, eig, hess);
+  });
+}
+
+int flygpu_hessian_eigenvalues_batch(flygpu_eam* eam, const flygpu_search_desc* systems, int n_systems,
+                                     const double* masses, int workers, double* eig) {
+  return guard([&] {
+    need(eam && eig && (systems || n_systems == 0), "null argument");
+    need(n_systems >= 0, "negative system count");
+    if (n_systems == 0) return;
+    std::vector<std::size_t> off(static_cast<std::size_t>(n_systems) + 1, 0);
+    for (int k = 0; k < n_systems; ++k) {
+      need(systems[k].n >= 0 && (systems[k].n == 0 || (systems[k].pos && systems[k].types && systems[k].frozen)),
+           "each system needs positions, types and frozen flags");
+      off[static_cast<std::size_t>(k) + 1] = off[static_cast<std::size_t>(k)] + 3 * static_cast<std::size_t>(systems[k].n);
+    }
+    int const P = std::max(1, std::min(workers > 0 ? workers : 8, n_systems));
+    std::vector<int> status(static_cast<std::size_t>(n_systems), FLYGPU_OK);
+    std::vector<std::string> msg(static_cast<std::size_t>(n_systems));
+    int dev = 0;
+    FLY_CUDA(cudaGetDevice(&dev));
+    auto work = [&](int w) {
+      // worker w: systems w, w + P, ... on its own stream, list and solver handle; every CUDA call sits
+      // inside guard (an exception must not leave the thread)
+      std::unique_ptr<flygpu_list> L;
+      for (int k = w; k < n_systems; k += P) {
+        flygpu_search_desc const& d = systems[k];
+        int const st = guard([&] {
+          FLY_CUDA(cudaSetDevice(dev));
+          if (!L) {
+            L = std::make_unique<flygpu_list>();
+            FLY_CUDA(cudaStreamCreateWithFlags(&L->stream, cudaStreamNonBlocking));
+            L->own_stream = true;
+            L->err.reserve(1);
+            L->counters.reserve(8);
+            L->h_small.reserve(8);
+            FLY_CUDA(cudaMemsetAsync(L->err.p, 0, sizeof(int), L->stream));
+          }
+          list_set_box(L.get(), d.extents, d.periodic, eam->r_cut);
+          if (d.n > 0) {
+            L->io.reserve(3 * static_cast<std::size_t>(d.n) + 3);
+            FLY_CUDA(cudaMemcpyAsync(L->io.p, d.pos, sizeof(double) * 3 * static_cast<std::size_t>(d.n),
+                                     cudaMemcpyHostToDevice, L->stream));
+          }
+          list_rebuild(L.get(), L->io.p, d.n);
+          check_device(L.get());
+          list_set_atoms(L.get(), eam->n_types, nullptr, nullptr, true, d.types, d.frozen);
+          if (d.n > 0) hessian_prefactor_one(eam, L.get(), d.types, d.frozen, masses, eig + off[static_cast<std::size_t>(k)], nullptr);
+        });
+        status[static_cast<std::size_t>(k)] = st;
+        if (st != FLYGPU_OK) msg[static_cast<std::size_t>(k)] = flygpu_last_error();
+      }
+      if (L) {
+        cudaStreamSynchronize(L->stream);
+        cudaStream_t const s = L->stream;
+        L.reset();
+        cudaStreamDestroy(s);
+      }
+    };
+    std::vector<std::thread> th;
+    for (int w = 1; w < P; ++w) th.emplace_back(work, w);
+    work(0);
+    for (auto& t : th) t.join();
+    for (int k = 0; k < n_systems; ++k)
+      if (status[static_cast<std::size_t>(k)] != FLYGPU_OK)
+        fail(status[static_cast<std::size_t>(k)], "system " + std::to_string(k) + ": " + msg[static_cast<std::size_t>(k)]);
   });
 }
 

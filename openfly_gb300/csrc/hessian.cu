@@ -228,23 +228,16 @@ namespace flygpu {
 
   }  // namespace
 
-  struct HessianPass {
-    DevBuf<long long> offs;
-    DevBuf<int> idx;
-    DevBuf<double> dr, rho_mu, fder;
-  };
-
   // Dense 3n x 3n Hessian into d_H (device, row-major). Synchronises the list's stream.
   void eam_hessian(flygpu_eam const* E, flygpu_list* L, double* d_H) {
     std::int64_t const n = L->n;
     cudaStream_t const s = L->stream;
     if (n == 0) return;
-    HessianPass P;
-    DevBuf<long long> offs0;
-    std::vector<int> const cnt = list_export_device(L, E->r_cut, offs0, P.idx, P.dr);
+    HessianScratch& P = L->hs;
+    P.offs.reserve(static_cast<std::size_t>(n) + 1);
+    std::vector<int> const cnt = list_export_device(L, E->r_cut, P.offs, P.idx, P.dr);
     std::vector<long long> ho(static_cast<std::size_t>(n) + 1, 0);
     for (std::int64_t i = 0; i < n; ++i) ho[static_cast<std::size_t>(i) + 1] = ho[static_cast<std::size_t>(i)] + cnt[static_cast<std::size_t>(i)];
-    P.offs.reserve(static_cast<std::size_t>(n) + 1);
     FLY_CUDA(cudaMemcpyAsync(P.offs.p, ho.data(), sizeof(long long) * ho.size(), cudaMemcpyHostToDevice, s));
     P.rho_mu.reserve(4 * static_cast<std::size_t>(n));
     P.fder.reserve(2 * static_cast<std::size_t>(n));
@@ -255,7 +248,7 @@ namespace flygpu {
            P.rho_mu.p, P.fder.p, L->err.p);
     launch(k_hess_col, static_cast<unsigned>((n + WARPS - 1) / WARPS), 32 * WARPS, 0, s, tb, n, P.offs.p, P.idx.p, P.dr.p,
            L->types.p, L->frozen.p, P.rho_mu.p, P.fder.p, d_H, L->err.p);
-    FLY_CUDA(cudaStreamSynchronize(s));  // P is freed on return
+    FLY_CUDA(cudaStreamSynchronize(s));  // the host vector ho stays alive until the copy has run
   }
 
   void hessian_mass_weight(flygpu_eam const* E, flygpu_list* L, double const* type_mass, std::uint32_t const* h_types,
@@ -271,7 +264,7 @@ namespace flygpu {
       if (!(m > 0)) fail(FLYGPU_INVALID_ARG, "masses must be positive");
       for (int k = 0; k < 3; ++k) m3[static_cast<std::size_t>(3 * i + k)] = m;
     }
-    DevBuf<double> dm;
+    DevBuf<double>& dm = L->hs.m3;
     dm.reserve(m3.size());
     FLY_CUDA(cudaMemcpyAsync(dm.p, m3.data(), sizeof(double) * m3.size(), cudaMemcpyHostToDevice, s));
     std::int64_t const N = 3 * n;
@@ -337,8 +330,8 @@ namespace flygpu {
     }
     std::vector<double> w(static_cast<std::size_t>(M));
     if (M > 0) {
-      DevBuf<int> d_act;
-      DevBuf<double> sub;
+      DevBuf<int>& d_act = L->hs.act;
+      DevBuf<double>& sub = L->hs.sub;
       d_act.reserve(static_cast<std::size_t>(M));
       sub.reserve(static_cast<std::size_t>(M * M));
       FLY_CUDA(cudaMemcpyAsync(d_act.p, act.data(), sizeof(int) * act.size(), cudaMemcpyHostToDevice, s));

@@ -190,6 +190,14 @@ namespace flygpu {
     float fp;
   };
 
+  // Device scratch of the Hessian calls, kept by the list handle so repeated calls allocate nothing (a
+  // cudaFree would synchronise the whole device and serialise concurrent callers).
+  struct HessianScratch {
+    DevBuf<long long> offs;
+    DevBuf<int> idx, act;
+    DevBuf<double> dr, rho_mu, fder, m3, sub, H;
+  };
+
 }  // namespace flygpu
 
 struct flygpu_list {
@@ -236,6 +244,8 @@ struct flygpu_list {
   bool timing = false;
   std::shared_ptr<void> solver;  // cuSOLVER handle of the Hessian eigensolves (created on first use)
   flygpu::DevBuf<double> solver_work;
+  flygpu::HessianScratch hs;
+  flygpu::DevBuf<int> export_counts;  // per-atom counts of list_export_device
   std::vector<cudaEvent_t> ev_pool;
   std::size_t ev_used = 0;
   struct Mark {
@@ -279,7 +289,8 @@ namespace flygpu {
 
   // hessian.cu: the dense 3n x 3n EAM Hessian into d_H (row-major, lower blocks); its mass weighting
   // (type_mass per type, NULL for the potential file's masses); the ascending eigenvalues of a symmetric
-  // matrix given by its row-major lower triangle (d_H is overwritten). Each synchronises the stream.
+  // matrix given by its row-major lower triangle (d_H is overwritten). Each synchronises the stream and
+  // keeps its scratch in L->hs.
   void eam_hessian(flygpu_eam const* E, flygpu_list* L, double* d_H);
   void hessian_mass_weight(flygpu_eam const* E, flygpu_list* L, double const* type_mass, std::uint32_t const* h_types,
                            double* d_H);

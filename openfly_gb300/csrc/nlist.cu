@@ -625,7 +625,7 @@ namespace flygpu {
     if (n == 0) return hc;
     cudaStream_t const s = L->stream;
     double const rc2 = r_cut * r_cut;
-    DevBuf<int> d_counts;
+    DevBuf<int>& d_counts = L->export_counts;
     d_counts.reserve(static_cast<std::size_t>(n));
     launch(k_export_count, blocks_for(n), T, 0, s, L->pos.p, L->real_phys.p, L->pimg.p, L->nbr.p, L->ncount.p, n, rc2,
            d_counts.p);

@@ -394,6 +394,24 @@ def minimise_system(eam: EAM, s: Search, precision: int = FP64, lbfgs: LBFGSOpti
     return r.as_dict(), out.reshape(-1, 3)
 
 
+def hessian_eigenvalues_batch(eam: EAM, systems: list, masses=None, workers: int = 8) -> list:
+    """The prefactor step (EAM::hessian + Hessian::mass_weight + Hessian::eigenvalues, find.cpp:838-871) for
+    many systems in one call (flygpu_hessian_eigenvalues_batch); returns each system's ascending
+    eigenvalues (3n,). systems: Search objects (positions, types, frozen, box; the search fields are not
+    used); masses per type (None: the potential file's)."""
+    _setup()
+    keep: list = []
+    descs = (SearchDesc * max(1, len(systems)))()
+    for k, s in enumerate(systems):
+        descs[k] = s.desc(keep)
+    sizes = [3 * s.n for s in systems]
+    eig = np.zeros(max(1, sum(sizes)), dtype=np.float64)
+    m = None if masses is None else np.ascontiguousarray(masses, dtype=np.float64)
+    check(lib().flygpu_hessian_eigenvalues_batch(eam.h, descs, len(systems), None if m is None else m.ctypes.data,
+                                                 workers, eig.ctypes.data), "Hessian batch")
+    return list(np.split(eig[: sum(sizes)], np.cumsum(sizes)[:-1])) if systems else []
+
+
 def search_plain(eam: EAM, s: Search, precision: int = FP64, dimer: DimerOptions | None = None,
                  lbfgs: LBFGSOptions | None = None):
     """One search the drop-in way; returns (result dict, positions (n,3), axis (n,3))."""

@@ -103,3 +103,28 @@ def test_spline_out_of_bounds_is_reported(gpu, geam):
     g.rebuild(ok)
     h = geam.hessian(np.zeros(2, np.uint32), np.zeros(2, np.uint8), g)
     assert h.shape == (6, 6) and np.isfinite(h).all()
+
+
+def test_batch_matches_single_calls_and_oracle(gpu, oracle, geam, odata):
+    # flygpu_hessian_eigenvalues_batch: 10 clusters of mixed sizes on 4 worker streams
+    from openfly_gb300 import search as S
+
+    clusters = W.search_clusters(n=10, seed=31)
+    systems = [S.from_cluster(c) for c in clusters]
+    batch = S.hessian_eigenvalues_batch(geam, systems, workers=4)
+    assert len(batch) == len(systems)
+    for c, ev in zip(clusters, batch):
+        s = c.sys
+        g, o = _pair(gpu, oracle, odata, s, odata.r_cut)
+        assert np.array_equal(ev, geam.hessian_eigenvalues(s.types, s.frozen, g))
+        ref = oracle.hessian_eigenvalues(oracle.eam_hessian(odata, o, s.types, s.frozen), _masses(odata, s.types))
+        assert np.abs(ev - ref).max() <= EIG_TOL * np.abs(ref).max()
+
+
+def test_batch_reports_the_failing_system(gpu, geam):
+    from openfly_gb300 import search as S
+
+    systems = [S.from_cluster(c) for c in W.search_clusters(n=3, seed=2)]
+    systems[1].types = np.full(systems[1].n, 7, np.uint32)  # no such type in the potential
+    with pytest.raises(gpu.FlyGPUError, match="system 1"):
+        S.hessian_eigenvalues_batch(geam, systems, workers=2)
