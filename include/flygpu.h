@@ -123,7 +123,8 @@ int flygpu_eam_energy_gradient_device(flygpu_eam* eam, flygpu_list* list, const 
  * Hessian of the list's atoms in binary64, row-major, the rows 3a..3a+2 belonging to atom a. As in the
  * reference only the lower 3x3 blocks (a >= z) are written, and the blocks of frozen atoms are zero;
  * the values are the reference's, bit for bit. types (n) and frozen (n) are required; hess: 9 n^2
- * doubles on the host. Neighbours are taken within the potential's cut-off from the list as built. */
+ * doubles on the host. Neighbours are taken within the potential's cut-off from the list as built.
+ * The list keeps the device scratch for the next call (the dense matrix only while it is at most 1 GiB). */
 int flygpu_eam_hessian(flygpu_eam* eam, flygpu_list* list, const uint32_t* types, const uint8_t* frozen,
                        double* hess);
 /* Hessian::mass_weight then Hessian::eigenvalues (system/hessian.hpp:86-93,136-143) of that Hessian,

@@ -102,6 +102,12 @@ namespace flygpu {
     hessian_eigenvalues(list, H.p, frozen, eig);
   }
 
+  // A list keeps its dense Hessian buffer between calls, except one above 1 GiB (a large system's matrix
+  // is not held after the call that needed it).
+  void release_large_hessian(flygpu_list* list) {
+    if (list->hs.H.n * sizeof(double) > (std::size_t{1} << 30)) list->hs.H.release();
+  }
+
   // The box and cut-off of a list (neigh::List::List, neigh/list.hpp:86-90; HyperGrid, hypergrid.hpp:43-53):
   // cell grid and the offset of the binary32 packed coordinates. The list must be rebuilt afterwards.
   void list_set_box(flygpu_list* L, double const extents[3], int const periodic[3], double r_cut) {
@@ -364,6 +370,7 @@ int flygpu_eam_hessian(flygpu_eam* eam, flygpu_list* list, const uint32_t* types
     check_device(list);
     FLY_CUDA(cudaMemcpyAsync(hess, H.p, sizeof(double) * N * N, cudaMemcpyDeviceToHost, list->stream));
     FLY_CUDA(cudaStreamSynchronize(list->stream));
+    release_large_hessian(list);
   });
 }
 
@@ -375,6 +382,7 @@ int flygpu_hessian_eigenvalues(flygpu_eam* eam, flygpu_list* list, const uint32_
     need(types && frozen, "types and frozen flags are required");
     list_set_atoms(list, eam->n_types, nullptr, nullptr, true, types, frozen);
     hessian_prefactor_one(eam, list, types, frozen, masses, eig, hess);
+    release_large_hessian(list);
   });
 }
 
