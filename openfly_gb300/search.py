@@ -426,3 +426,145 @@ def search_plain(eam: EAM, s: Search, precision: int = FP64, dimer: DimerOptions
     check(lib().flygpu_search_plain(eam.h, C.byref(dimer), C.byref(lbfgs), precision, C.byref(d), pos.ctypes.data,
                                     ax.ctypes.data, C.byref(r)), "search_plain")
     return r.as_dict(), pos.reshape(-1, 3), ax.reshape(-1, 3)
+
+
+class MasterOptions:
+    """The Master::Options fields the mechanism step reads (saddle/find.hpp:100-160), with the reference's
+    defaults."""
+
+    def __init__(self, basin_tol: float = 0.05, stationary_tol: float | None = None, capture_r_tol: float = 0.05,
+                 capture_E_tol: float = 0.01, hessian_eigen_zero_tol: float = 1e-6, nudge_frac: float = 0.01):
+        self.basin_tol = basin_tol
+        self.stationary_tol = basin_tol / 2 if stationary_tol is None else stationary_tol
+        self.capture_r_tol = capture_r_tol
+        self.capture_E_tol = capture_E_tol
+        self.hessian_eigen_zero_tol = hessian_eigen_zero_tol
+        self.nudge_frac = nudge_frac
+
+
+def _modes(freq: np.ndarray, tol: float):
+    """Counts of the sorted eigenvalues: (negative, zero, sum of log of the positive ones)."""
+    neg = int((freq < -tol).sum())
+    pos = freq[freq > tol]
+    return neg, int(freq.size - neg - pos.size), float(np.sum(np.log(pos)))
+
+
+def minimum_modes(eam: EAM, minima: list[Search], masses=None, opts: MasterOptions | None = None) -> list[dict]:
+    """Master::calc_minima_hess (find.cpp:1094-1144) for each minimum: the log product of the non-zero
+    mass-weighted Hessian eigenvalues and the number of zero modes. Raises, as the reference's verify,
+    on a negative mode or a zero-mode count other than 3 per frozen atom (3 when none is frozen)."""
+    opts = opts or MasterOptions()
+    out = []
+    for s, freq in zip(minima, hessian_eigenvalues_batch(eam, minima, masses)):
+        neg, zeros, logp = _modes(freq, opts.hessian_eigen_zero_tol)
+        if neg:
+            raise RuntimeError(f"Mode 0 has eigenvalue = {freq[0]}")
+        n_frozen = int(np.asarray(s.frozen).sum())
+        expect = 3 * n_frozen if n_frozen > 0 else 3
+        if zeros != expect:
+            raise RuntimeError(f"Expecting {expect} zero modes but found {zeros}")
+        out.append(dict(log_prod_eigen=logp, zero_modes=zeros, count_frozen=n_frozen))
+    return out
+
+
+def mechanisms(eam: EAM, saddles: list[Search], minima: list[np.ndarray], geos: list, masses=None,
+               opts: MasterOptions | None = None, precision: int = MIXED, dimer: DimerOptions | None = None,
+               lbfgs: LBFGSOptions | None = None, zero_modes: list[int] | None = None,
+               tuning: Tuning | None = None) -> list:
+    """Master::saddle_2_mech (find.cpp:757-981) for many saddles, every relaxation batched on the device.
+
+    For saddle k (positions = the converged dimer, axis = its axis, types/frozen = the initial minimum's)
+    with initial minimum minima[k] and local geometry geos[k] (atom indices, the centre first):
+    do_adj_min (`pathways`); no mechanism if rev lies more than basin_tol from the initial minimum,
+    fwd within basin_tol of rev, or the saddle within stationary_tol of rev or fwd (:771-797); the
+    barrier E_sp - E_rev (which must be positive) and delta E_fwd - E_rev; the saddle and final-state
+    displacements and the normalised axis on the geometry's atoms (:807-836); the prefactor from the
+    saddle's mass-weighted Hessian (:838-871): exactly one negative mode (a second one: no mechanism),
+    the zero modes counted against zero_modes[k] (default: the initial minimum's, `minimum_modes`) and
+    kinetic_pre = sum of the log of the positive eigenvalues; and recon_relax (:77-125, :874-956): the
+    mechanism rebuilt on rev, the minimum relaxed with LBFGS::minimise and the saddle with Dimer::find_sp,
+    each compared (after centroid alignment) with the pathway's fwd and saddle within capture_r_tol and
+    capture_E_tol (poison_fwd / poison_sp). Raises where the reference throws (a non-positive barrier, no
+    negative mode, a wrong zero-mode count, a poisoned final state with a barrier under 0.5 eV).
+    Returns per saddle None or a dict of the mechanism."""
+    opts = opts or MasterOptions()
+    dimer = dimer or DimerOptions.defaults()
+    lbfgs = lbfgs or LBFGSOptions.defaults()
+    centres = [int(g[0]) for g in geos]
+    paths = pathways(eam, saddles, minima, centres, precision=precision, nudge_frac=opts.nudge_frac, lbfgs=lbfgs,
+                     tuning=tuning)
+    keep = []
+    for k, p in enumerate(paths):
+        if p is None:
+            continue
+        x0 = np.asarray(minima[k], np.float64).reshape(-1, 3)
+        rev, sp, fwd = p["rev"], p["sp"], p["fwd"]
+        if (np.linalg.norm(rev - x0) > opts.basin_tol or np.linalg.norm(fwd - rev) < opts.basin_tol
+                or np.linalg.norm(rev - sp) < opts.stationary_tol or np.linalg.norm(fwd - sp) < opts.stationary_tol):
+            continue
+        if not p["E_sp"] > p["E_rev"]:
+            raise RuntimeError(f"Bad internal state Esp={p['E_sp']} but E0={p['E_rev']}!")
+        keep.append(k)
+    if zero_modes is None and keep:
+        mins = [Search(minima[k], saddles[k].types, saddles[k].frozen, saddles[k].extents, saddles[k].periodic)
+                for k in keep]
+        zero_modes = {k: m["zero_modes"] for k, m in zip(keep, minimum_modes(eam, mins, masses, opts))}
+    elif zero_modes is not None:
+        zero_modes = {k: zero_modes[k] for k in keep}
+    # prefactors at the saddles (one batched call)
+    sps = [Search(paths[k]["sp"], saddles[k].types, saddles[k].frozen, saddles[k].extents, saddles[k].periodic)
+           for k in keep]
+    freqs = dict(zip(keep, hessian_eigenvalues_batch(eam, sps, masses))) if keep else {}
+    mech = {}
+    for k in keep:
+        p, geo = paths[k], np.asarray(geos[k], np.int64)
+        freq = freqs[k]
+        tol = opts.hessian_eigen_zero_tol
+        if not freq[0] < -tol:
+            raise RuntimeError(f"Saddle-point with minimum mode={freq[0]}")
+        neg, zeros, logp = _modes(freq[1:], tol)
+        if neg:
+            continue  # second-order saddle point or higher
+        if zeros != zero_modes[k]:
+            raise RuntimeError(f"Expecting {zero_modes[k]} zero modes but hessian has {zeros}")
+        ax = np.asarray(saddles[k].axis, np.float64).reshape(-1, 3)[geo]
+        mech[k] = dict(barrier=p["E_sp"] - p["E_rev"], delta=p["E_fwd"] - p["E_rev"],
+                       delta_sp=p["sp"][geo] - p["rev"][geo], delta_fwd=p["fwd"][geo] - p["rev"][geo],
+                       axis=ax / np.sqrt((ax * ax).sum()), kinetic_pre=logp, geo=geo,
+                       rev=p["rev"], sp=p["sp"], fwd=p["fwd"], E_rev=p["E_rev"], E_sp=p["E_sp"], E_fwd=p["E_fwd"])
+    # recon_relax: rebuild every mechanism on its rev and relax both states (one batched launch)
+    reqs, slots = [], []
+    for k, m in mech.items():
+        s, ref = saddles[k], m["rev"]
+        re_min, re_sp = ref.copy(), ref.copy()
+        re_min[m["geo"]] += m["delta_fwd"]
+        re_sp[m["geo"]] += m["delta_sp"]
+        if int(np.asarray(s.frozen).sum()) == 0:
+            re_sp = centroid_align(re_sp, ref)
+        axis = np.zeros_like(ref)
+        axis[m["geo"]] = m["axis"]
+        m["re_min"], m["re_sp"] = re_min, re_sp
+        slots.append(k)
+        reqs.append(Search(re_min, s.types, s.frozen, s.extents, s.periodic, mode=MINIMISE))
+        reqs.append(Search(re_sp, s.types, s.frozen, s.extents, s.periodic, axis=axis, in_min=ref))
+    if reqs:
+        b = Batch(eam, reqs, precision=precision, dimer=dimer, lbfgs=lbfgs)
+        b.run(tuning)
+        res, pos, _ = b.results()
+    out = [None] * len(saddles)
+    for j, k in enumerate(slots):
+        m = mech[k]
+        for which, r, x, ref_x, e_ref in (("fwd", res[2 * j], pos[2 * j], m["fwd"], m["E_fwd"]),
+                                            ("sp", res[2 * j + 1], pos[2 * j + 1], m["sp"], m["E_sp"])):
+            if r["status"] != 0 or r["exit_code"] != 0:
+                m["poison_" + which], m["err_" + which] = True, None
+                continue
+            m["err_" + which] = float(np.linalg.norm(x - m["re_min" if which == "fwd" else "re_sp"]))
+            aligned = centroid_align(x, ref_x)
+            m["poison_" + which] = bool(np.linalg.norm(aligned - ref_x) > opts.capture_r_tol
+                                        or abs(r["energy"] - e_ref) > opts.capture_E_tol)
+        if m["poison_fwd"] and m["barrier"] < 0.5:
+            raise RuntimeError(f"Mechanism @{int(m['geo'][0])} with energy barrier = {m['barrier']}eV is poisoned! "
+                               f"err_sp={m['err_sp']}, err_min={m['err_fwd']}")
+        out[k] = m
+    return out

@@ -461,3 +461,106 @@ def cell_idx(extents, r_cut: float, x) -> int:
     """HyperGrid(extents, r_cut).cell_idx(x) (system/boxes/hypergrid.hpp:43-99)."""
     return lib().orc_cell_idx(np.ascontiguousarray(extents, dtype=np.float64), r_cut,
                               np.ascontiguousarray(x, dtype=np.float64))
+
+
+def _energy_at(data: EAMData, extents, periodic, pos, types) -> float:
+    nl = List(extents, periodic, data.r_cut)
+    nl.rebuild(np.asarray(pos, np.float64), 1)
+    return eam_energy(data, nl, types)
+
+
+def _frequencies(data: EAMData, extents, periodic, pos, types, frozen, masses) -> np.ndarray:
+    nl = List(extents, periodic, data.r_cut)
+    nl.rebuild(np.asarray(pos, np.float64), 1)
+    return hessian_eigenvalues(eam_hessian(data, nl, types, frozen), masses)
+
+
+def minimum_modes(data: EAMData, extents, periodic, pos, types, frozen, masses, tol: float = 1e-6) -> dict:
+    """Master::calc_minima_hess (saddle/find.cpp:1094-1144): log product of the non-zero eigenvalues and the
+    zero-mode count; raises on a negative mode or a count other than 3 per frozen atom (3 when none)."""
+    freq = _frequencies(data, extents, periodic, pos, types, frozen, masses)
+    logp, zeros = 0.0, 0
+    for i in range(freq.size):
+        if not freq[i] > -tol:
+            raise RuntimeError(f"Mode {i} has eigenvalue = {freq[i]}")
+        if freq[i] > tol:
+            logp += float(np.log(freq[i]))
+        else:
+            zeros += 1
+    n_frozen = int(np.asarray(frozen).sum())
+    expect = 3 * n_frozen if n_frozen > 0 else 3
+    if zeros != expect:
+        raise RuntimeError(f"Expecting {expect} zero modes but found {zeros}")
+    return dict(log_prod_eigen=logp, zero_modes=zeros)
+
+
+def mechanism(data: EAMData, dimer_opt: DimerOptions, lbfgs_opt: LBFGSOptions, extents, periodic, types, frozen,
+              in_pos, sp_pos, sp_axis, geo, masses, zero_modes: int, basin_tol: float = 0.05,
+              stationary_tol: float = 0.025, capture_r_tol: float = 0.05, capture_e_tol: float = 0.01,
+              zero_tol: float = 1e-6, nudge_frac: float = 0.01):
+    """Master::saddle_2_mech (saddle/find.cpp:757-981) with recon_relax (:77-125) for one saddle: the
+    pathway (adj_min) and its checks (:771-797), the three energies on rebuilt lists (:801-810), the
+    mechanism on the geometry's atoms (:812-836), the prefactor (:838-871) and the reconstruction onto
+    rev with its poison tests (:874-956). Returns None where the reference returns no mechanism; raises
+    where it throws."""
+    geo = np.asarray(geo, np.int64)
+    path = adj_min(data, lbfgs_opt, extents, periodic, types, frozen, sp_pos, sp_axis, in_pos, int(geo[0]),
+                   nudge_frac)
+    if path is None:
+        return None
+    x0 = np.asarray(in_pos, np.float64).reshape(-1, 3)
+    rev, sp, fwd = path["rev"], path["sp"], path["fwd"]
+    if np.linalg.norm(rev - x0) > basin_tol or np.linalg.norm(fwd - rev) < basin_tol:
+        return None
+    if np.linalg.norm(rev - sp) < stationary_tol or np.linalg.norm(fwd - sp) < stationary_tol:
+        return None
+    e0 = _energy_at(data, extents, periodic, rev, types)
+    esp = _energy_at(data, extents, periodic, sp, types)
+    ef = _energy_at(data, extents, periodic, fwd, types)
+    if not esp > e0:
+        raise RuntimeError(f"Bad internal state Esp={esp} but E0={e0}!")
+    ax = np.asarray(sp_axis, np.float64).reshape(-1, 3)[geo]
+    s = 0.0
+    for a in ax:
+        s += float(a @ a)
+    m = dict(barrier=esp - e0, delta=ef - e0, delta_sp=sp[geo] - rev[geo], delta_fwd=fwd[geo] - rev[geo],
+             axis=ax / np.sqrt(s), rev=rev, sp=sp, fwd=fwd)
+    freq = _frequencies(data, extents, periodic, sp, types, frozen, masses)
+    if not freq[0] < -zero_tol:
+        raise RuntimeError(f"Saddle-point with minimum mode={freq[0]}")
+    pre, zeros = 0.0, 0
+    for i in range(1, freq.size):
+        if freq[i] < -zero_tol:
+            return None
+        if freq[i] > zero_tol:
+            pre += float(np.log(freq[i]))
+        else:
+            zeros += 1
+    if zeros != zero_modes:
+        raise RuntimeError(f"Expecting {zero_modes} zero modes but hessian has {zeros}")
+    m["kinetic_pre"] = pre
+    # recon_relax onto rev
+    re_min, re_sp = rev.copy(), rev.copy()
+    re_min[geo] += m["delta_fwd"]
+    re_sp[geo] += m["delta_sp"]
+    n_frozen = int(np.asarray(frozen).sum())
+    if n_frozen == 0:
+        re_sp = re_sp + (rev.mean(axis=0) - re_sp.mean(axis=0))
+    axis = np.zeros_like(rev)
+    axis[geo] = m["axis"]
+    failed, _, rel_min, _ = lbfgs_minimise(data, lbfgs_opt, extents, periodic, re_min, types, frozen)
+    d = dimer_find_sp(data, dimer_opt, extents, periodic, re_sp, axis, types, frozen, in_min=rev,
+                      count_frozen=n_frozen)
+    for which, ok, x, base, ref_x, e_ref in (("fwd", not failed, rel_min, re_min, fwd, ef),
+                                             ("sp", d["exit"] == 0, d["x"], re_sp, sp, esp)):
+        if not ok:
+            m["poison_" + which], m["err_" + which] = True, None
+            continue
+        x = np.asarray(x, np.float64).reshape(-1, 3)
+        m["err_" + which] = float(np.linalg.norm(x - base))
+        x = x + (ref_x.mean(axis=0) - x.mean(axis=0))
+        e = _energy_at(data, extents, periodic, x, types)
+        m["poison_" + which] = bool(np.linalg.norm(x - ref_x) > capture_r_tol or abs(e - e_ref) > capture_e_tol)
+    if m["poison_fwd"] and m["barrier"] < 0.5:
+        raise RuntimeError(f"Mechanism @{int(geo[0])} with energy barrier = {m['barrier']}eV is poisoned!")
+    return m
