@@ -331,8 +331,55 @@ def search_metrics(fly, args) -> dict:
     out["served"]["plain_service_p50_ms"] = out["batched"]["plain_one_at_a_time"]["p50_ms"]
     out["served"]["plain_service_p99_ms"] = out["batched"]["plain_one_at_a_time"]["p99_ms"]
     out["served"]["saturated"] = serve_run(S, eam, stream, tune, opt, args, None)
+    out["mechanisms"] = mechanism_metrics(fly, eam, S, W)
     out["gpu_launches"] = int(fly.launch_count() - l0)
     return out
+
+
+def mechanism_metrics(fly, eam, S, W, n: int = 256) -> dict:
+    """Master's post-search pipeline on n search clusters, as Master runs it: each cluster relaxed to its
+    minimum, perturbed around its centre (Master::perturb) and climbed to a saddle (binary32 pairs, one
+    batched launch each); then search.mechanisms (saddle_2_mech: do_adj_min, the checks, energies,
+    prefactors and recon_relax, all relaxations batched) on the converged saddles, timed on its own.
+    Each saddle's geometry is centred on the atom that moves most in its pathway."""
+    clusters = W.search_clusters(n=n, seed=19)
+    lb = S.LBFGSOptions.defaults(f2norm=1e-6)
+    relax = S.Batch(eam, [S.from_cluster(c, mode=S.MINIMISE) for c in clusters], precision=fly.MIXED, lbfgs=lb)
+    relax.run()
+    _, minima, _ = relax.results()
+    rng = np.random.default_rng(5)
+    starts = []
+    for c, x in zip(clusters, minima):
+        s = c.sys
+        p, a = W.perturb(W.System(x, s.types, s.frozen, s.extents, s.periodic), c.centre, rng)
+        starts.append(S.Search(p, s.types, s.frozen, s.extents, s.periodic, axis=a, in_min=x))
+    opt = S.DimerOptions.defaults(n=6, rot_n=6, f2norm=1e-3, max_steps=1000)
+    b = S.Batch(eam, starts, precision=fly.MIXED, dimer=opt)
+    b.run()
+    res, pos, ax = b.results()
+    found = [(c, x, S.Search(xs, c.sys.types, c.sys.frozen, c.sys.extents, c.sys.periodic, axis=a))
+             for c, x, r, xs, a in zip(clusters, minima, res, pos, ax) if r["status"] == 0 and r["exit_code"] == 0]
+    paths = S.pathways(eam, [s for *_, s in found], [x for _, x, _ in found], None, precision=fly.MIXED, lbfgs=lb)
+    sel, geos = [], []
+    for (c, x, s), p in zip(found, paths):
+        if p is not None:
+            mm = int(np.argmax(((p["rev"] - p["fwd"]) ** 2).sum(axis=1)))
+            d = np.linalg.norm(x - x[mm], axis=1)
+            geos.append(np.concatenate([[mm], np.flatnonzero((d < 4.0) & (np.arange(c.sys.n) != mm))]))
+            sel.append((c, x, s))
+    t0 = time.perf_counter()
+    try:
+        mech = S.mechanisms(eam, [s for *_, s in sel], [x for _, x, _ in sel], geos, precision=fly.MIXED, dimer=opt,
+                            lbfgs=lb)
+        err = None
+    except RuntimeError as e:  # a verify() of the reference (kept as the reference raises it)
+        mech, err = [], str(e)
+    dt = time.perf_counter() - t0
+    built = [m for m in mech if m is not None]
+    return {"clusters": n, "saddles": len(sel), "mechanisms": len(built), "seconds": dt,
+            "saddles_per_s": len(sel) / dt if dt > 0 else None,
+            "poisoned": sum(1 for m in built if m["poison_sp"] or m["poison_fwd"]), "raised": err,
+            "note": "search.mechanisms: saddle_2_mech for every saddle; relaxations, Hessians and recon batched"}
 
 
 # ----------------------------------------------------------------------------- GPU leg
