@@ -428,6 +428,9 @@ def search_plain(eam: EAM, s: Search, precision: int = FP64, dimer: DimerOptions
     return r.as_dict(), pos.reshape(-1, 3), ax.reshape(-1, 3)
 
 
+AMU_KG = 1.6605390666050e-27  # the atomic mass unit in kg, as find.cpp:288 writes it
+
+
 class MasterOptions:
     """The Master::Options fields the mechanism step reads (saddle/find.hpp:100-160), with the reference's
     defaults."""
@@ -481,7 +484,9 @@ def mechanisms(eam: EAM, saddles: list[Search], minima: list[np.ndarray], geos: 
     displacements and the normalised axis on the geometry's atoms (:807-836); the prefactor from the
     saddle's mass-weighted Hessian (:838-871): exactly one negative mode (a second one: no mechanism),
     the zero modes counted against zero_modes[k] (default: the initial minimum's, `minimum_modes`) and
-    kinetic_pre = sum of the log of the positive eigenvalues; and recon_relax (:77-125, :874-956): the
+    kinetic_pre = sum of the log of the positive eigenvalues, and with the minimum's log product the
+    prefactor sqrt(exp(log_prod_min - kinetic_pre) / (2 pi amu)) in Hz (find.cpp:286-292; None when
+    zero_modes is given); and recon_relax (:77-125, :874-956): the
     mechanism rebuilt on rev, the minimum relaxed with LBFGS::minimise and the saddle with Dimer::find_sp,
     each compared (after centroid alignment) with the pathway's fwd and saddle within capture_r_tol and
     capture_E_tol (poison_fwd / poison_sp). Raises where the reference throws (a non-positive barrier, no
@@ -505,10 +510,13 @@ def mechanisms(eam: EAM, saddles: list[Search], minima: list[np.ndarray], geos: 
         if not p["E_sp"] > p["E_rev"]:
             raise RuntimeError(f"Bad internal state Esp={p['E_sp']} but E0={p['E_rev']}!")
         keep.append(k)
+    log_prod = {}
     if zero_modes is None and keep:
         mins = [Search(minima[k], saddles[k].types, saddles[k].frozen, saddles[k].extents, saddles[k].periodic)
                 for k in keep]
-        zero_modes = {k: m["zero_modes"] for k, m in zip(keep, minimum_modes(eam, mins, masses, opts))}
+        mm = minimum_modes(eam, mins, masses, opts)
+        zero_modes = {k: m["zero_modes"] for k, m in zip(keep, mm)}
+        log_prod = {k: m["log_prod_eigen"] for k, m in zip(keep, mm)}
     elif zero_modes is not None:
         zero_modes = {k: zero_modes[k] for k in keep}
     # prefactors at the saddles (one batched call)
@@ -531,6 +539,8 @@ def mechanisms(eam: EAM, saddles: list[Search], minima: list[np.ndarray], geos: 
         mech[k] = dict(barrier=p["E_sp"] - p["E_rev"], delta=p["E_fwd"] - p["E_rev"],
                        delta_sp=p["sp"][geo] - p["rev"][geo], delta_fwd=p["fwd"][geo] - p["rev"][geo],
                        axis=ax / np.sqrt((ax * ax).sum()), kinetic_pre=logp, geo=geo,
+                       prefactor_hz=(float(np.sqrt(np.exp(log_prod[k] - logp) / (2 * np.pi * AMU_KG)))
+                                     if k in log_prod else None),
                        rev=p["rev"], sp=p["sp"], fwd=p["fwd"], E_rev=p["E_rev"], E_sp=p["E_sp"], E_fwd=p["E_fwd"])
     # recon_relax: rebuild every mechanism on its rev and relax both states (one batched launch)
     reqs, slots = [], []

@@ -77,6 +77,10 @@ def test_mechanisms_match_oracle(gpu, oracle, geam, odata, saddles):
         assert np.abs(m["delta_fwd"] - ref["delta_fwd"]).max() < DELTA_A
         assert np.abs(m["axis"] - ref["axis"]).max() < 1e-12
         assert abs(m["kinetic_pre"] - ref["kinetic_pre"]) < PRE_ABS
+        # the prefactor in Hz (find.cpp:286-292) from the minimum's and the saddle's log products
+        lp = oracle.minimum_modes(odata, sy.extents, sy.periodic, x, sy.types, sy.frozen, masses)["log_prod_eigen"]
+        hz = np.sqrt(np.exp(lp - ref["kinetic_pre"]) / (2 * np.pi * 1.6605390666050e-27))
+        assert abs(m["prefactor_hz"] / hz - 1) < 2 * PRE_ABS
         assert m["poison_sp"] == ref["poison_sp"] and m["poison_fwd"] == ref["poison_fwd"]
     assert built >= 2
 
