@@ -1,7 +1,8 @@
 """Writes tests/golden/reference_kats.json: the known answers of the reference's own tests for this path.
 
 Reads the reference's test sources as text (it cannot be compiled here) and extracts:
-  tests/potential/EAM/eam.cpp   E0 (line 119), grad_0 (line 125), perfect-lattice |grad| bound (line 167)
+  tests/potential/EAM/eam.cpp   E0 (line 119), grad_0 (line 125), perfect-lattice |grad| bound (line 167),
+                                the Hessian block H(0,0) of the erased cell and its tolerance (lines 131-141)
   tests/potential/EAM/data.cpp  f_Fe(0), f_Fe(0.02) (lines 42-43)
   tests/neigh/adjacent.cpp      AdjacentCells of a 5^3 grid: interior order, face/edge/corner counts
   tests/system/boxes/hypergrid.cpp  HyperGrid(10, 3).cell_idx at 0, 5, 9.5
@@ -40,6 +41,11 @@ def main() -> None:
     kat["grad0_component"] = float(re.search(r"Vec::Constant\(([-0-9.eE+]+)\)\)\s*<\s*1e-10", eam).group(1))
     kat["grad0_tol"] = 1e-10
     kat["perfect_grad_norm_max"] = float(re.search(r"gnorm\(cell\[g_\]\)\s*<\s*([-0-9.eE+]+)", eam).group(1))
+    block = re.search(r"Mat ngd = Mat\{(.*?)\};", eam, re.S).group(1)
+    rows = re.findall(r"\{([^{}]*)\}", block)
+    kat["hessian_block_00"] = [[float(v) for v in r.split(",") if v.strip()] for r in rows]
+    assert len(kat["hessian_block_00"]) == 3 and all(len(r) == 3 for r in kat["hessian_block_00"])
+    kat["hessian_block_tol"] = float(re.search(r"gnorm\(ngd - H\(0, 0\)\)\s*<\s*([-0-9.eE+]+)", eam).group(1))
     fvals = re.findall(r"data\.f\(0\)\.f\(([-0-9.eE+]+)\),\s*([-0-9.eE+]+)\)", data)
     kat["f_Fe"] = [[float(x), float(y)] for x, y in fvals]
     interior = [arith(e) for e in re.findall(r"REQUIRE\(neigh\[\d+\]\s*==\s*([^;]+)\);", adj)]

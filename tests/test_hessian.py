@@ -1,15 +1,17 @@
 """The oracle's EAM Hessian and eigenvalue restatements (eam.cpp:122-233, system/hessian.hpp:86-143),
 pinned to the reference's known answers and to finite differences of the pinned gradient. CPU only."""
+import json
+import os
+
 import numpy as np
 
 from openfly_gb300 import workloads as W
 
-# tests/potential/EAM/eam.cpp:131-135, the (0, 0) block of the erased 7x7x7 cell
-KAT_H00 = np.array([
-    [+9.0654715551510830, -1.0875103661087880, -1.0875103661087877],
-    [-1.0875103661087880, +9.0654715551510830, -1.0875103661087873],
-    [-1.0875103661087877, -1.0875103661087873, +9.0654715551510830],
-])
+# tests/potential/EAM/eam.cpp:131-141, the (0, 0) block of the erased 7x7x7 cell and its tolerance, as
+# extracted from the reference's test source into the golden fixture (tests/golden/make_golden.py)
+_KATS = json.load(open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "reference_kats.json")))
+KAT_H00 = np.array(_KATS["hessian_block_00"])
+KAT_H00_TOL = _KATS["hessian_block_tol"]
 
 
 def near(a, b, atol=1e-10, ftol=1e-4):
@@ -26,7 +28,7 @@ def _hess(oracle, odata, s, rc=None):
 def test_kat_block_away_from_minimum(oracle, odata):
     # tests/potential/EAM/eam.cpp:98-146
     _, h = _hess(oracle, odata, W.kat_lattice())
-    assert np.linalg.norm(h[:3, :3] - KAT_H00) < 1e-10
+    assert np.linalg.norm(h[:3, :3] - KAT_H00) < KAT_H00_TOL
 
 
 def test_kat_zero_modes_at_minimum(oracle, odata):
