@@ -4,6 +4,7 @@ restatement (oracle.mechanism) on saddles of binary64 cluster searches."""
 import numpy as np
 import pytest
 
+from openfly_gb300 import search as S
 from openfly_gb300 import workloads as W
 
 pytestmark = pytest.mark.gpu
@@ -11,18 +12,17 @@ pytestmark = pytest.mark.gpu
 BARRIER_EV = 1e-5     # barrier and delta of the same pathway
 DELTA_A = 1e-3        # displacements of the geometry's atoms
 PRE_ABS = 1e-3        # kinetic_pre, a sum of ~100-300 log eigenvalues
+SHAPE = S.Tuning(4, 128, 2, 0)  # a fixed launch shape: results must not depend on the autotuner's timing
 
 
 @pytest.fixture(scope="module")
 def saddles(gpu, geam):
     # As Master does: relax each cluster to its minimum, perturb around the centre (Master::perturb) and
     # climb from there (binary64 throughout, so the device and the oracle follow the same pathways).
-    from openfly_gb300 import search as S
-
     clusters = W.search_clusters(n=24, seed=11)
     lb = S.LBFGSOptions.defaults(f2norm=1e-6)
     relax = S.Batch(geam, [S.from_cluster(c, mode=S.MINIMISE) for c in clusters], precision=gpu.FP64, lbfgs=lb)
-    relax.run()
+    relax.run(SHAPE)
     _, minima, _ = relax.results()
     rng = np.random.default_rng(5)
     starts = []
@@ -33,13 +33,14 @@ def saddles(gpu, geam):
         starts.append(S.Search(p, s.types, s.frozen, s.extents, s.periodic, axis=a, in_min=x))
     opt = S.DimerOptions.defaults(n=6, rot_n=6, f2norm=1e-5, max_steps=1000)
     b = S.Batch(geam, starts, precision=gpu.FP64, dimer=opt)
-    b.run()
+    b.run(SHAPE)
     res, pos, ax = b.results()
     found = [(c, x, S.Search(xs, c.sys.types, c.sys.frozen, c.sys.extents, c.sys.periodic, axis=a))
              for c, x, r, xs, a in zip(clusters, minima, res, pos, ax) if r["status"] == 0 and r["exit_code"] == 0]
     # Master keeps a mechanism only in the environment of the atom that moves most (find.cpp:1082-1087): each
     # saddle's geometry is centred on that atom of its pathway (the atom and its neighbours within 4 A)
-    paths = S.pathways(geam, [s for *_, s in found], [x for _, x, _ in found], None, precision=gpu.FP64, lbfgs=lb)
+    paths = S.pathways(geam, [s for *_, s in found], [x for _, x, _ in found], None, precision=gpu.FP64, lbfgs=lb,
+                       tuning=SHAPE)
     out = []
     for (c, x, s), p in zip(found, paths):
         if p is None:
@@ -53,11 +54,9 @@ def saddles(gpu, geam):
 
 
 def test_mechanisms_match_oracle(gpu, oracle, geam, odata, saddles):
-    from openfly_gb300 import search as S
-
     found, opt, lb = saddles
     mechs = S.mechanisms(geam, [s for _, _, s, _ in found], [x for _, x, _, _ in found], [g for *_, g in found],
-                         precision=gpu.FP64, dimer=opt, lbfgs=lb)
+                         precision=gpu.FP64, dimer=opt, lbfgs=lb, tuning=SHAPE)
     odim = oracle.DimerOptions.defaults(n=6, rot_n=6, f2norm=1e-5, max_steps=1000)
     olb = oracle.LBFGSOptions.defaults(f2norm=1e-6)
     built = 0
@@ -87,8 +86,6 @@ def test_mechanisms_match_oracle(gpu, oracle, geam, odata, saddles):
 
 def test_minimum_modes(gpu, oracle, geam, odata):
     # Master::calc_minima_hess on a relaxed cluster: 3 zero modes per frozen atom, the same log product
-    from openfly_gb300 import search as S
-
     c = W.search_clusters(n=1, seed=3)[0]
     s = c.sys
     _, x = S.minimise_system(geam, S.Search(s.pos, s.types, s.frozen, s.extents, s.periodic, mode=S.MINIMISE),
