@@ -81,3 +81,24 @@ def test_centroid_align():
     y = S.centroid_align(x, w)
     assert np.allclose(S.centroid(y), S.centroid(w), atol=1e-12)
     assert np.allclose(y - x, (S.centroid(w) - S.centroid(x))[None, :])
+
+
+def test_master_options_defaults():
+    # saddle/find.hpp:112,120,129,138,163,184
+    from openfly_gb300 import search as S
+
+    o = S.MasterOptions()
+    assert (o.basin_tol, o.stationary_tol, o.capture_r_tol, o.capture_E_tol) == (0.05, 0.025, 0.05, 0.01)
+    assert (o.hessian_eigen_zero_tol, o.nudge_frac) == (1e-6, 0.01)
+    assert S.MasterOptions(basin_tol=0.2).stationary_tol == 0.1  # stationary_tol = basin_tol / 2
+
+
+def test_mode_classification():
+    # the eigenvalue loops of find.cpp:851-865 and :1116-1126: negative below -tol, zero within tol,
+    # the log of the rest summed
+    from openfly_gb300 import search as S
+
+    freq = np.array([-2.0, -1e-7, 0.0, 5e-7, 1.0, np.e])
+    neg, zeros, logp = S._modes(freq, 1e-6)
+    assert (neg, zeros) == (1, 3)
+    assert np.isclose(logp, 1.0)
