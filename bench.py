@@ -73,7 +73,7 @@ def schedule(steps: int):
 class Clocks:
     """nvidia-smi sampling during the timed region."""
 
-    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    Q = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
@@ -81,12 +81,13 @@ class Clocks:
         self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
         try:
             self.p = subprocess.Popen(["nvidia-smi", f"--id={index}", f"--query-gpu={self.Q}",
-                                       "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                       "--format=csv,noheader,nounits", "-lms", "100"], stdout=self.f,
                                       stderr=subprocess.DEVNULL)
         except OSError:
             self.p = None
 
-    def stop(self) -> dict | None:
+    def stop(self, t0: float, t1: float) -> dict | None:
+        """Summary of the samples whose timestamps fall in the timed region [t0, t1] (host time.time())."""
         if self.p is None:
             return None
         self.p.terminate()
@@ -94,13 +95,18 @@ class Clocks:
         self.f.flush()
         rows = [r.split(",") for r in open(self.f.name).read().strip().splitlines() if r.strip()]
         os.unlink(self.f.name)
+        import datetime
+
         sm, mx, reasons = [], 0.0, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for r in rows:
             try:
-                sm.append(float(r[1]))
-                mx = max(mx, float(r[2]))
-                for name, v in zip(names, r[5:9]):
+                ts = datetime.datetime.strptime(r[0].strip(), "%Y/%m/%d %H:%M:%S.%f").timestamp()
+                if not t0 <= ts <= t1:
+                    continue
+                sm.append(float(r[2]))
+                mx = max(mx, float(r[3]))
+                for name, v in zip(names, r[6:10]):
                     if v.strip() == "Active":
                         reasons.add(name)
             except (ValueError, IndexError):
@@ -433,6 +439,8 @@ def ours(args):
             nl.update_device(d_fields[j] if sign > 0 else d_neg[j])
         eam.energy_gradient_device(nl, d_e, d_grad, precision=fly.MIXED)
 
+    clocks = Clocks(local)  # started early: nvidia-smi takes a moment to produce its first sample
+    time.sleep(0.5)
     for j, sign, rb in schedule(args.warmup):
         step(j, sign, rb)
     nl.sync()
@@ -440,18 +448,19 @@ def ours(args):
     if dist:
         tdist.barrier()
     torch.cuda.synchronize()
-    clocks = Clocks(local)
     nl.set_timing(True)
     launches0 = fly.launch_count()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t_clk0 = time.time()
     ev0.record(stream)
     for j, sign, rb in sched:
         step(j, sign, rb)
     ev1.record(stream)
     torch.cuda.synchronize()
+    t_clk1 = time.time()
     launches = fly.launch_count() - launches0
     ktimes = nl.kernel_times()
-    clk = clocks.stop()
+    clk = clocks.stop(t_clk0, t_clk1)
     nl.sync()
     ms = reduce_max(ev0.elapsed_time(ev1), dev)
     value = replica_value(n, world, args.steps, ms)
@@ -568,6 +577,7 @@ def ours(args):
     if rank == 0 and not args.no_cpu and world == 1:
         threads = os.cpu_count() or 1
         os.environ.setdefault("OMP_NUM_THREADS", str(threads))
+        cpu_crystal_steps(s, fields, 1, threads)  # warm-up: OpenMP threads and first-touch pages
         secs, k, rb = cpu_crystal_steps(s, fields, args.cpu_steps, threads)
         line["cpu_baseline"] = {"value": n * k / secs, "unit": "atom-evals/s", "cores": threads, "kind": "port",
                                 "sample": f"{k} steps ({rb} rebuild) of the same {n}-atom workload, oracle port, "
@@ -703,11 +713,11 @@ def search_tail(args) -> None:
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=60)
+    ap.add_argument("--steps", type=int, default=600)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--cells", type=int, default=80, help="bcc cells per side (80 -> 1,024,000 sites)")
-    ap.add_argument("--cpu-steps", type=int, default=3, help="steps of the bounded CPU baseline sample")
+    ap.add_argument("--cpu-steps", type=int, default=5, help="steps of the bounded CPU baseline sample")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-searches", action="store_true", help="skip the search metrics (configs 3 and 4)")
     ap.add_argument("--searches", type=int, default=4096, help="clusters in the batched search run")
