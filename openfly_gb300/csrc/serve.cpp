@@ -216,20 +216,20 @@ void flygpu_server::retire() {
     if (!sl.busy || h_S.p[s].stage != STAGE_DONE) continue;
     Request& r = *sl.req;
     std::size_t const M = 3 * static_cast<std::size_t>(h_S.p[s].na);
-    Out o{s, std::vector<double>(M), std::vector<double>(M)};
+    Out out{s, std::vector<double>(M), std::vector<double>(M)};
     double const* vec = reinterpret_cast<double const*>(sl.block + r.layout.vec);
-    FLY_CUDA(cudaMemcpyAsync(o.x.data(), vec + V_X * M, M * sizeof(double), cudaMemcpyDeviceToHost, copy));
-    if (r.mode == MODE_DIMER) FLY_CUDA(cudaMemcpyAsync(o.ax.data(), vec + V_AX * M, M * sizeof(double), cudaMemcpyDeviceToHost, copy));
+    FLY_CUDA(cudaMemcpyAsync(out.x.data(), vec + V_X * M, M * sizeof(double), cudaMemcpyDeviceToHost, copy));
+    if (r.mode == MODE_DIMER) FLY_CUDA(cudaMemcpyAsync(out.ax.data(), vec + V_AX * M, M * sizeof(double), cudaMemcpyDeviceToHost, copy));
     FLY_CUDA(cudaFreeAsync(sl.block, copy));
-    outs.push_back(std::move(o));
+    outs.push_back(std::move(out));
   }
   if (outs.empty()) return;
   FLY_CUDA(cudaStreamSynchronize(copy));
   auto const now = Clock::now();
-  for (Out& o : outs) {
-    Slot& sl = slots[o.slot];
+  for (Out& fin : outs) {
+    Slot& sl = slots[fin.slot];
     Request& r = *sl.req;
-    SearchDev const& d = h_S.p[o.slot];
+    SearchDev const& d = h_S.p[fin.slot];
     Finished f;
     f.info.id = r.id;
     f.info.result.exit_code = d.exit_code;
@@ -243,8 +243,8 @@ void flygpu_server::retire() {
     for (std::size_t k = 0; k < r.mob.size(); ++k)
       for (std::size_t c = 0; c < 3; ++c) {
         std::size_t const a = 3 * static_cast<std::size_t>(r.mob[k]) + c;
-        f.pos[a] = o.x[3 * k + c];
-        if (r.mode == MODE_DIMER) f.axis[a] = o.ax[3 * k + c];
+        f.pos[a] = fin.x[3 * k + c];
+        if (r.mode == MODE_DIMER) f.axis[a] = fin.ax[3 * k + c];
       }
     f.info.latency_ms = ms_since(r.t_submit, now);
     f.info.queue_ms = ms_since(r.t_submit, r.t_admit);
