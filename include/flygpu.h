@@ -268,6 +268,9 @@ int flygpu_server_create(flygpu_eam* eam, const flygpu_dimer_options* dimer, con
 void flygpu_server_destroy(flygpu_server* srv);
 /* Queues one search (inputs are copied); id receives its request id. */
 int flygpu_server_submit(flygpu_server* srv, const flygpu_search_desc* desc, uint64_t* id);
+/* n searches in one call, all or none: every descriptor is checked first (an invalid one, reported with
+ * its index, queues nothing), then they are queued in order with consecutive ids (ids: n entries). */
+int flygpu_server_submit_many(flygpu_server* srv, const flygpu_search_desc* descs, int n, uint64_t* ids);
 /* Returns up to max finished searches, waiting up to wait_ms for the first. */
 int flygpu_server_poll(flygpu_server* srv, int max, int wait_ms, flygpu_served* out, int* n_out);
 /* Copies a polled search's final positions / axis (3n each, may be NULL) and forgets it. */

@@ -343,25 +343,50 @@ int flygpu_server_create(flygpu_eam* eam, const flygpu_dimer_options* dimer, con
 
 void flygpu_server_destroy(flygpu_server* srv) { delete srv; }
 
-int flygpu_server_submit(flygpu_server* srv, const flygpu_search_desc* desc, uint64_t* id) {
-  return guard([&] {
-    if (!srv || !desc) fail(FLYGPU_INVALID_ARG, "null argument");
+namespace {
+
+  // A request from its descriptor (validated, host copies of its arrays); throws on a bad descriptor.
+  std::unique_ptr<Request> make_request(flygpu_server* srv, flygpu_search_desc const& desc) {
     auto r = std::make_unique<Request>();
     r->t_submit = Clock::now();
-    r->layout = search_prepare(srv->o, srv->eam->n_types, *desc, r->S, r->mob, r->image, 0);
-    r->mode = desc->mode;
-    r->pos.assign(desc->pos, desc->pos + 3 * desc->n);
-    if (desc->mode == FLYGPU_SEARCH_DIMER) {
-      r->axis.assign(desc->axis, desc->axis + 3 * desc->n);
+    r->layout = search_prepare(srv->o, srv->eam->n_types, desc, r->S, r->mob, r->image, 0);
+    r->mode = desc.mode;
+    r->pos.assign(desc.pos, desc.pos + 3 * desc.n);
+    if (desc.mode == FLYGPU_SEARCH_DIMER) {
+      r->axis.assign(desc.axis, desc.axis + 3 * desc.n);
     } else {
-      r->axis.assign(static_cast<std::size_t>(3 * desc->n), 0.0);
+      r->axis.assign(static_cast<std::size_t>(3 * desc.n), 0.0);
     }
     if (static_cast<std::int64_t>(r->layout.total) > srv->budget) fail(FLYGPU_OOM, "request larger than the HBM budget");
+    return r;
+  }
+
+}  // namespace
+
+int flygpu_server_submit(flygpu_server* srv, const flygpu_search_desc* desc, uint64_t* id) {
+  return flygpu_server_submit_many(srv, desc, 1, id);
+}
+
+int flygpu_server_submit_many(flygpu_server* srv, const flygpu_search_desc* descs, int n, uint64_t* ids) {
+  return guard([&] {
+    if (!srv || (n > 0 && !descs) || n < 0) fail(FLYGPU_INVALID_ARG, "null argument or negative count");
+    std::vector<std::unique_ptr<Request>> reqs;
+    reqs.reserve(static_cast<std::size_t>(n));
+    for (int k = 0; k < n; ++k) {
+      try {
+        reqs.push_back(make_request(srv, descs[k]));
+      } catch (Error const& e) {
+        fail(e.status, "request " + std::to_string(k) + ": " + e.msg);
+      }
+    }
     std::lock_guard<std::mutex> lk(srv->mu);
     if (srv->error != FLYGPU_OK) fail(srv->error, "server stopped: " + srv->error_msg);
-    r->id = srv->next_id++;
-    if (id) *id = r->id;
-    srv->pending.push_back(std::move(r));
+    for (int k = 0; k < n; ++k) {
+      auto& r = reqs[static_cast<std::size_t>(k)];
+      r->id = srv->next_id++;
+      if (ids) ids[k] = r->id;
+      srv->pending.push_back(std::move(r));
+    }
     srv->cv_work.notify_one();
   });
 }

@@ -241,6 +241,7 @@ class Server:
         L.flygpu_server_create.argtypes = [V, V, V, C.c_int, C.c_int64, C.c_int, C.c_int, V, C.POINTER(V)]
         L.flygpu_server_destroy.argtypes = [V]
         L.flygpu_server_submit.argtypes = [V, V, C.POINTER(C.c_uint64)]
+        L.flygpu_server_submit_many.argtypes = [V, V, C.c_int, V]
         L.flygpu_server_poll.argtypes = [V, C.c_int, C.c_int, V, C.POINTER(C.c_int)]
         L.flygpu_server_take.argtypes = [V, C.c_uint64, V, V]
         L.flygpu_server_get_stats.argtypes = [V, V]
@@ -269,6 +270,19 @@ class Server:
         check(lib().flygpu_server_submit(self.h, C.byref(d), C.byref(rid)), "Server.submit")
         self.n_atoms[rid.value] = s.n
         return rid.value
+
+    def submit_many(self, searches: list[Search]) -> list[int]:
+        """flygpu_server_submit_many: all of them or none; returns their ids in order."""
+        keep: list = []
+        descs = (SearchDesc * max(1, len(searches)))()
+        for k, x in enumerate(searches):
+            descs[k] = x.desc(keep)
+        ids = np.zeros(max(1, len(searches)), dtype=np.uint64)
+        check(lib().flygpu_server_submit_many(self.h, descs, len(searches), ids.ctypes.data), "Server.submit_many")
+        out = [int(i) for i in ids[: len(searches)]]
+        for rid, x in zip(out, searches):
+            self.n_atoms[rid] = x.n
+        return out
 
     def poll(self, max_n: int = 256, wait_ms: int = 0) -> list[dict]:
         buf = (Served * max_n)()

@@ -83,3 +83,30 @@ def test_request_over_budget_is_rejected(gpu, geam, S, requests):
         srv.submit(S.from_cluster(requests[0]))
     assert e.value.status == gpu.OOM
     srv.close()
+
+
+def test_submit_many_is_all_or_nothing(gpu, geam, S, requests):
+    # flygpu_server_submit_many: results equal single submissions; a bad descriptor queues none of them
+    opt = S.DimerOptions.defaults(f2norm=1e-3, n=6)
+    t = S.Tuning(4, 128, 2)
+    sub = requests[:6]
+    single, _ = serve_all(S, gpu, geam, sub, opt, t)
+    srv = S.Server(geam, precision=gpu.MIXED, hbm_budget_bytes=1 << 30, max_active=64, tuning=t, dimer=opt)
+    bad = [S.from_cluster(c) for c in sub]
+    bad[3].types = np.full(bad[3].n, 200, np.uint32)  # no such type in the potential
+    with pytest.raises(gpu.FlyGPUError, match="request 3"):
+        srv.submit_many(bad)
+    st = srv.stats()
+    assert st["pending"] == 0 and st["active"] == 0 and st["completed"] == 0
+    ids = srv.submit_many([S.from_cluster(c) for c in sub])
+    assert ids == sorted(ids) and len(set(ids)) == len(sub)
+    got = {}
+    t0 = time.time()
+    while len(got) < len(ids) and time.time() - t0 < 120:
+        for r in srv.poll(64, wait_ms=50):
+            got[r["id"]] = (r, *srv.take(r["id"]))
+    srv.close()
+    assert len(got) == len(ids)
+    for i, x in zip(ids, single):
+        assert got[i][0]["energy"] == x[0]["energy"]
+        assert np.array_equal(got[i][1], x[1])
