@@ -11,6 +11,7 @@
 //   neigh/adjacent.hpp:40-70                                          (AdjacentCells)
 //   src/neigh/list.cpp:37-165, neigh/list.hpp:78,139-154              (List)
 //   src/potential/EAM/eam.cpp:33-120                                  (EAM energy / gradient)
+//   src/potential/EAM/eam.cpp:122-233                                 (EAM::hessian)
 //   src/minimise/LBFGS/lbfgs_core.cpp:29-87                           (StepLBFGS)
 //   src/minimise/LBFGS/lbfgs.cpp:29-115                               (LBFGS::minimise)
 //   src/saddle/rotor.cpp:33-164                                       (trans_proj, Rotor::eff_gradient)
@@ -23,7 +24,7 @@
 //   * the squared length of a 3-vector is (x*x + y*y) + z*z (Eigen's packet-of-two reduction order);
 //   * long reductions (gdot/gnorm over 3N, sums over atoms) are sequential in index order.
 // The reference's own build may contract to FMA and vectorise reductions; its known-answer tests
-// (tests/potential/EAM/eam.cpp:119,125, tests/potential/EAM/data.cpp:42-43) pin this oracle.
+// (tests/potential/EAM/eam.cpp:119,125,141,173-183, tests/potential/EAM/data.cpp:42-43) pin this oracle.
 //
 // Errors: every entry point returns an int status (0 = ok, 1 = invalid argument, 2 = spline out of
 // bounds, 3 = ghost capacity exceeded).

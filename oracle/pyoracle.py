@@ -2,6 +2,12 @@
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the CPU legs of bench.py as
 the checker. The product package never imports this module.
+
+Beyond the C++ restatements it restates in Python the host-side glue of Master (saddle/find.cpp):
+do_adj_min (:1014-1090, `adj_min`), saddle_2_mech with recon_relax (:757-981, :77-125, `mechanism`),
+calc_minima_hess (:1094-1144, `minimum_modes`), the catalogue's local environments
+(env/catalogue.cpp:66-78, `local_environment`) and Hessian::mass_weight / eigenvalues
+(system/hessian.hpp:86-93,136-143).
 """
 from __future__ import annotations
 
