@@ -1,5 +1,5 @@
 """The host logic of search.mechanisms (Master::saddle_2_mech, find.cpp:757-981, with recon_relax,
-:77-125) without a GPU: the device calls it makes (pathways, the batched Hessian eigenvalues and the
+:77-125) and search.pathways (do_adj_min, :1014-1090) without a GPU: the device calls it makes (pathways, the batched Hessian eigenvalues and the
 batched relaxations) are replaced by stand-ins returning chosen values, so each of the reference's
 branches is reached on purpose."""
 import numpy as np
@@ -132,3 +132,54 @@ def test_poisoned_low_barrier_raises(monkeypatch):
     _setup(monkeypatch, _path(E_sp=-9.8), GOOD_SP, GOOD_MIN, {"min": (far, -9.9, 0), "sp": (SP, -9.8, 0)})
     with pytest.raises(RuntimeError, match="poisoned"):
         _run()
+
+
+class FakeRelax:
+    """Stands in for search.Batch inside pathways: the + nudged relaxation ends at `plus`, the - nudged
+    one at `minus` (plus a uniform drift), and the zero-step energy batch reports e["sp"]."""
+
+    plus = minus = None
+    drift = np.zeros(3)
+    e = dict(plus=-9.9, minus=-10.0, sp=-9.5)
+    code = 0
+
+    def __init__(self, eam, reqs, lbfgs=None, **kw):
+        self.reqs, self.energy_only = reqs, lbfgs is not None and lbfgs.iter_max == 0
+
+    def run(self, tuning=None):
+        pass
+
+    def results(self, positions=True):
+        if self.energy_only:
+            return [dict(status=0, exit_code=0, energy=self.e["sp"])] * len(self.reqs), None, None
+        res, pos = [], []
+        for k in range(len(self.reqs)):
+            which = "plus" if k % 2 == 0 else "minus"
+            res.append(dict(status=0, exit_code=self.code, energy=self.e[which]))
+            pos.append(getattr(self, which) + self.drift)
+        return res, pos, [None] * len(self.reqs)
+
+
+def _paths(monkeypatch, plus, minus, drift=(0.0, 0.0, 0.0), centre=0, code=0):
+    FakeRelax.plus, FakeRelax.minus, FakeRelax.drift, FakeRelax.code = plus, minus, np.asarray(drift), code
+    monkeypatch.setattr(S, "Batch", FakeRelax)
+    return S.pathways(None, [_saddle()], [MINIMUM], [centre])[0]
+
+
+def test_pathways_assigns_rev_and_removes_drift(monkeypatch):
+    # find.cpp:1054-1075: the relaxed state nearer the initial minimum is rev; rev's centroid drift from the
+    # minimum is removed from all three states
+    p = _paths(monkeypatch, plus=FWD, minus=REV, drift=(0.05, -0.02, 0.01))
+    assert np.allclose(p["rev"], REV) and np.allclose(p["fwd"], FWD)
+    assert np.allclose(p["sp"], SP - np.array([0.05, -0.02, 0.01]))
+    assert (p["E_rev"], p["E_fwd"], p["E_sp"]) == (-10.0, -9.9, -9.5) and p["barrier"] == pytest.approx(0.5)
+    q = _paths(monkeypatch, plus=REV, minus=FWD)  # the other way round: still rev = the nearer one
+    assert np.allclose(q["rev"], REV) and q["E_rev"] == -9.9
+
+
+def test_pathways_centre_and_failure(monkeypatch):
+    # find.cpp:1082-1087: the atom moving most between rev and fwd must be the centre (atom 0 here)
+    assert _paths(monkeypatch, plus=FWD, minus=REV, centre=1) is None
+    assert _paths(monkeypatch, plus=FWD, minus=REV, centre=0) is not None
+    # a relaxation that does not converge gives no pathway (find.cpp:1038-1050)
+    assert _paths(monkeypatch, plus=FWD, minus=REV, code=1) is None
