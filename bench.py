@@ -710,6 +710,17 @@ def search_tail(args) -> None:
                       "max_grad_calls": int(max(r["grad_calls"] for r in r2))}), flush=True)
 
 
+def prefactor_only(args) -> None:
+    """Only the prefactor step (hessian_prefactor: one 610-atom cluster, then a batch of 32), for
+    profiling the Hessian kernels; prints one JSON line (not a bench line)."""
+    import openfly_gb300 as fly
+    from openfly_gb300 import workloads as W
+    from openfly_gb300.build import build
+
+    build()
+    print(json.dumps({"prefactor": hessian_prefactor(fly, fly.EAM(W.TABLE))}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--gpus", type=int, default=1)
@@ -728,6 +739,8 @@ def main():
                     help="only run one batch of this many cluster searches (a small case for profilers)")
     ap.add_argument("--max-search-steps", type=int, default=1000, help="translation-step limit of --search-batch")
     ap.add_argument("--precision", choices=["mixed", "fp64"], default="mixed", help="precision of --search-batch")
+    ap.add_argument("--prefactor", action="store_true",
+                    help="only run the Hessian prefactor step (profiling the Hessian kernels)")
     ap.add_argument("--search-tail", action="store_true",
                     help="only run the searches of a cluster batch that outlast 100 steps, in one launch (profiling)")
     args = ap.parse_args()
@@ -735,6 +748,9 @@ def main():
         ap.error("--warmup must be at least 3")
     if args.search_tail:
         search_tail(args)
+        return
+    if args.prefactor:
+        prefactor_only(args)
         return
     if args.search_batch > 0:
         search_batch(args)
