@@ -92,7 +92,7 @@ namespace flygpu {
     if (N == 0) return;
     DevBuf<double>& H = list->hs.H;
     H.reserve(N * N);
-    eam_hessian(eam, list, H.p);
+    eam_hessian(eam, list, frozen, H.p);
     check_device(list);
     hessian_mass_weight(eam, list, masses, types, H.p);
     if (hess) {
@@ -366,7 +366,7 @@ int flygpu_eam_hessian(flygpu_eam* eam, flygpu_list* list, const uint32_t* types
     if (N == 0) return;
     DevBuf<double>& H = list->hs.H;
     H.reserve(N * N);
-    eam_hessian(eam, list, H.p);
+    eam_hessian(eam, list, frozen, H.p);
     check_device(list);
     FLY_CUDA(cudaMemcpyAsync(hess, H.p, sizeof(double) * N * N, cudaMemcpyDeviceToHost, list->stream));
     FLY_CUDA(cudaStreamSynchronize(list->stream));

@@ -2,7 +2,7 @@
 //
 // Restates EAM::hessian (src/potential/EAM/eam.cpp:122-233) on the device. Pass 1, one thread per atom
 // b (active and frozen): rho_b = sum_a phi(t_a, t_b)(r) and mu_b = -sum_a phi'(t_a, t_b)(r) dr / r
-// (A.13), with F'(rho_b) and F''(rho_b). Pass 2, one warp per active atom z, writes only column block z
+// (A.13), with F'(rho_b) and F''(rho_b). Pass 2, one warp (CTA) per active atom z, writes only column block z
 // of the dense 3n x 3n matrix (row-major; the rows of atom a are 3a..3a+2):
 //   H(z,z) = F''_z mu_z mu_z^T + sum_a [A 1 - ABFpp dr dr^T]                           (A.15, A.14)
 //   H(a,z) += -BArr dr dr^T - A 1 + ur dr mu_z^T - ru mu_a dr^T       for active a > z
@@ -111,16 +111,15 @@ namespace flygpu {
       if (bad) atomicOr(err, ERR_SPLINE_OOB);
     }
 
-    constexpr int WARPS = 4;
-
-    // Pass 2: column block z, one warp per active atom z.
-    __global__ void __launch_bounds__(32 * WARPS)
-        k_hess_col(TablesView tb, std::int64_t n, long long const* __restrict__ offs, int const* __restrict__ idx,
-                   double const* __restrict__ dr, std::uint32_t const* __restrict__ types,
+    // Pass 2: column block z, one 32-thread CTA per active atom (cols lists them), so the columns spread
+    // over the SMs whatever the atoms' numbering.
+    __global__ void __launch_bounds__(32)
+        k_hess_col(TablesView tb, std::int64_t n, int const* __restrict__ cols, long long const* __restrict__ offs,
+                   int const* __restrict__ idx, double const* __restrict__ dr, std::uint32_t const* __restrict__ types,
                    std::uint8_t const* __restrict__ frozen, double const* __restrict__ rho_mu,
                    double const* __restrict__ fder, double* __restrict__ H, int* __restrict__ err) {
-      std::int64_t const z = static_cast<std::int64_t>(blockIdx.x) * WARPS + (threadIdx.x >> 5);
-      int const lane = threadIdx.x & 31;
+      std::int64_t const z = cols[blockIdx.x];
+      int const lane = threadIdx.x;
       if (z >= n || frozen[z]) return;
       std::int64_t const N = 3 * n;
       auto at = [&](std::int64_t i, std::int64_t j, int r, int c) -> double& { return H[(3 * i + r) * N + 3 * j + c]; };
@@ -229,11 +228,17 @@ namespace flygpu {
   }  // namespace
 
   // Dense 3n x 3n Hessian into d_H (device, row-major). Synchronises the list's stream.
-  void eam_hessian(flygpu_eam const* E, flygpu_list* L, double* d_H) {
+  void eam_hessian(flygpu_eam const* E, flygpu_list* L, std::uint8_t const* h_frozen, double* d_H) {
     std::int64_t const n = L->n;
     cudaStream_t const s = L->stream;
     if (n == 0) return;
     HessianScratch& P = L->hs;
+    std::vector<int> cols;
+    for (std::int64_t i = 0; i < n; ++i)
+      if (!h_frozen[i]) cols.push_back(static_cast<int>(i));
+    P.cols.reserve(std::max<std::size_t>(cols.size(), 1));
+    if (!cols.empty())
+      FLY_CUDA(cudaMemcpyAsync(P.cols.p, cols.data(), sizeof(int) * cols.size(), cudaMemcpyHostToDevice, s));
     P.offs.reserve(static_cast<std::size_t>(n) + 1);
     std::vector<int> const cnt = list_export_device(L, E->r_cut, P.offs, P.idx, P.dr);
     std::vector<long long> ho(static_cast<std::size_t>(n) + 1, 0);
@@ -246,9 +251,10 @@ namespace flygpu {
     TablesView const tb = E->view();
     launch(k_hess_rho, static_cast<unsigned>((n + 127) / 128), 128, 0, s, tb, n, P.offs.p, P.idx.p, P.dr.p, L->types.p,
            P.rho_mu.p, P.fder.p, L->err.p);
-    launch(k_hess_col, static_cast<unsigned>((n + WARPS - 1) / WARPS), 32 * WARPS, 0, s, tb, n, P.offs.p, P.idx.p, P.dr.p,
-           L->types.p, L->frozen.p, P.rho_mu.p, P.fder.p, d_H, L->err.p);
-    FLY_CUDA(cudaStreamSynchronize(s));  // the host vector ho stays alive until the copy has run
+    if (!cols.empty())
+      launch(k_hess_col, static_cast<unsigned>(cols.size()), 32, 0, s, tb, n, P.cols.p, P.offs.p, P.idx.p, P.dr.p,
+             L->types.p, L->frozen.p, P.rho_mu.p, P.fder.p, d_H, L->err.p);
+    FLY_CUDA(cudaStreamSynchronize(s));  // the host vectors ho and cols stay alive until their copies have run
   }
 
   void hessian_mass_weight(flygpu_eam const* E, flygpu_list* L, double const* type_mass, std::uint32_t const* h_types,

@@ -194,7 +194,7 @@ namespace flygpu {
   // cudaFree would synchronise the whole device and serialise concurrent callers).
   struct HessianScratch {
     DevBuf<long long> offs;
-    DevBuf<int> idx, act;
+    DevBuf<int> idx, act, cols;
     DevBuf<double> dr, rho_mu, fder, m3, sub, H;
   };
 
@@ -291,7 +291,7 @@ namespace flygpu {
   // (type_mass per type, NULL for the potential file's masses); the ascending eigenvalues of a symmetric
   // matrix given by its row-major lower triangle (d_H is overwritten). Each synchronises the stream and
   // keeps its scratch in L->hs.
-  void eam_hessian(flygpu_eam const* E, flygpu_list* L, double* d_H);
+  void eam_hessian(flygpu_eam const* E, flygpu_list* L, std::uint8_t const* h_frozen, double* d_H);
   void hessian_mass_weight(flygpu_eam const* E, flygpu_list* L, double const* type_mass, std::uint32_t const* h_types,
                            double* d_H);
   // The solver handle and workspace are the list's (L->solver, L->solver_work), on the list's stream.
