@@ -102,3 +102,14 @@ def test_mode_classification():
     neg, zeros, logp = S._modes(freq, 1e-6)
     assert (neg, zeros) == (1, 3)
     assert np.isclose(logp, 1.0)
+
+
+def test_bench_replica_value_and_traffic_table():
+    import bench
+
+    # N replicas, each n atoms x K steps, over the slowest rank's time (whole-job weak-scaling throughput)
+    assert bench.replica_value(1000, 4, 10, 2.0) == pytest.approx(1000 * 4 * 10 / 2e-3)
+    # the committed per-atom DRAM traffic of the binary32 passes, scaled to the bench's atom count
+    t = bench.traffic_from_profile("k_force32", 1_000_000)
+    assert t is not None and 200e6 < t < 400e6
+    assert bench.traffic_from_profile("no_such_kernel", 10) is None
