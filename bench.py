@@ -431,6 +431,12 @@ def ours(args):
     nl.rebuild_device(d_pos0, n)
     eam.energy_gradient_device(nl, d_e, d_grad, d_types=d_types, d_frozen=d_frozen, precision=fly.MIXED)
     nl.sync()
+    # untimed: both precisions' gradients and energies at the workload's positions, for the parity
+    # block the CPU leg fills in against the oracle's binary64 gradient on the same positions
+    par = {"mixed": (float(d_e.item()), d_grad.cpu().numpy().reshape(-1, 3))}
+    eam.energy_gradient_device(nl, d_e, d_grad, precision=fly.FP64)
+    nl.sync()
+    par["fp64"] = (float(d_e.item()), d_grad.cpu().numpy().reshape(-1, 3))
 
     def step(j, sign, rb):
         if rb:
@@ -582,6 +588,7 @@ def ours(args):
         line["cpu_baseline"] = {"value": n * k / secs, "unit": "atom-evals/s", "cores": threads, "kind": "port",
                                 "sample": f"{k} steps ({rb} rebuild) of the same {n}-atom workload, oracle port, "
                                           f"{threads} OpenMP threads"}
+        line["parity"] = parity_block(s, par, threads)
         from oracle import pyoracle as O
 
         olmin = O.LBFGSOptions.defaults(iter_max=3, f2norm=1e-9)
@@ -612,6 +619,33 @@ def ours(args):
         print(json.dumps(line), flush=True)
     if dist:
         tdist.destroy_process_group()
+
+
+def parity_block(s, par, threads: int) -> dict:
+    """The headline workload's gradient and energy against the oracle's binary64 EAM::gradient / energy on
+    the same positions (the CPU leg's oracle port): binary32 pairs within the stated tolerance, binary64
+    bit for bit."""
+    from oracle import pyoracle as O
+    from openfly_gb300 import workloads as W
+
+    od = O.EAMData(W.TABLE)
+    ol = O.List(s.extents, s.periodic, od.r_cut + SKIN)
+    ol.rebuild(s.pos, threads)
+    ref = O.eam_gradient(od, ol, s.types, s.frozen, threads)
+    e_ref = O.eam_energy(od, ol, s.types, threads)
+    e32, g32 = par["mixed"]
+    e64, g64 = par["fp64"]
+    err = np.abs(g32 - ref)
+    big = np.abs(ref) >= 1e-2
+    return {"atoms": s.n, "against": "oracle binary64 EAM::gradient/energy on the same positions",
+            "mixed": {"grad_norm_rel": float(np.linalg.norm(g32 - ref) / np.linalg.norm(ref)),
+                      "grad_max_abs_eV_per_A": float(err.max()),
+                      "grad_max_component_rel": float((err[big] / np.abs(ref[big])).max()),
+                      "grad_p99_component_rel": float(np.percentile(err[big] / np.abs(ref[big]), 99)),
+                      "energy_err_eV_per_atom": abs(e32 - e_ref) / s.n,
+                      "tolerance": "norm-wise relative 1e-6 (component relative over components >= 1e-2 eV/A)"},
+            "fp64": {"grad_bit_identical": bool(np.array_equal(g64, ref)),
+                     "energy_rel": abs(e64 - e_ref) / abs(e_ref)}}
 
 
 def HESS_SYSTEM():

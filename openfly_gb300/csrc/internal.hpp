@@ -142,12 +142,20 @@ namespace flygpu {
     float4 phi, v;
   };
 
+  // Derivative record of the same (t_i, t_n, interval) for the binary32 force pass: v_{t_i t_n} and
+  // phi_{t_n -> t_i} as {b_hi, b_lo, 2c, 3d} in the unit coordinate (b = b_hi + b_lo to ~2^-48, so
+  // df/dt = b_hi + (b_lo + t (2c + 3 t d)) carries no rounding of its leading coefficient).
+  struct alignas(32) DerRec {
+    float4 v, phi;
+  };
+
   // Device view passed to kernels by value.
   struct TablesView {
     int n_types;
     int nP, nR;  // intervals of F and of phi / v
     double dP, inv_dP, dR, inv_dR;
     float fdP, finv_dP, fdR, finv_dR;
+    float finv_dR_lo;  // 1/dR - finv_dR: 1/dR as a binary32 pair
     D4 const* F64;
     D4 const* phi64;  // [a + n*b] * nR
     D4 const* v64;    // both orders filled
@@ -155,6 +163,7 @@ namespace flygpu {
     float4 const* phi32;
     float4 const* v32;
     PairRec const* pv32;  // [t_i * n_types + t_n] * nR + interval
+    DerRec const* dv32;   // same indexing
   };
 
 }  // namespace flygpu
@@ -166,6 +175,7 @@ struct flygpu_eam {
   std::vector<double> mass;
   flygpu::SplineSet F, phi, v;  // phi and v hold n*n functions (v symmetric, both orders)
   flygpu::DevBuf<flygpu::PairRec> pv;  // phi and v of each ordered type pair merged per interval
+  flygpu::DevBuf<flygpu::DerRec> dv;   // their derivative records
   flygpu::TablesView view() const;
 };
 

@@ -86,6 +86,17 @@ namespace flygpu {
       return f32;
     }
 
+    // Derivative coefficients of interval k in the unit coordinate: {b_hi, b_lo, 2c, 3d} with b = b dx,
+    // c = c dx^2, d = d dx^3 formed in binary64 and b split into a binary32 pair.
+    float4 unit_deriv32(SplineSet const& s, std::size_t k) {
+      double const* c = &s.host[4 * k];
+      double const dx = s.dx;
+      double const b = c[1] * dx;
+      float const bh = static_cast<float>(b);
+      return make_float4(bh, static_cast<float>(b - static_cast<double>(bh)), static_cast<float>(2 * c[2] * dx * dx),
+                         static_cast<float>(3 * c[3] * dx * dx * dx));
+    }
+
     void upload(SplineSet& s) {
       std::size_t const total = static_cast<std::size_t>(s.count) * static_cast<std::size_t>(s.n_spines);
       std::vector<float4> const f32 = unit32(s);
@@ -112,6 +123,7 @@ flygpu::TablesView flygpu_eam::view() const {
   t.finv_dP = static_cast<float>(F.inv_dx);
   t.fdR = static_cast<float>(phi.dx);
   t.finv_dR = static_cast<float>(phi.inv_dx);
+  t.finv_dR_lo = static_cast<float>(phi.inv_dx - static_cast<double>(t.finv_dR));
   t.F64 = F.d64.p;
   t.phi64 = phi.d64.p;
   t.v64 = v.d64.p;
@@ -119,6 +131,7 @@ flygpu::TablesView flygpu_eam::view() const {
   t.phi32 = phi.d32.p;
   t.v32 = v.d32.p;
   t.pv32 = pv.p;
+  t.dv32 = dv.p;
   return t;
 }
 
@@ -192,6 +205,16 @@ namespace flygpu {
           }
       E->pv.reserve(rec.size());
       FLY_CUDA(cudaMemcpy(E->pv.p, rec.data(), rec.size() * sizeof(PairRec), cudaMemcpyHostToDevice));
+      std::vector<DerRec> der(rec.size());
+      for (int ti = 0; ti < nt; ++ti)
+        for (int tn = 0; tn < nt; ++tn)
+          for (std::size_t i = 0; i < nR; ++i) {
+            DerRec& r = der[(static_cast<std::size_t>(ti) * nt + tn) * nR + i];
+            r.v = unit_deriv32(E->v, (static_cast<std::size_t>(ti) + static_cast<std::size_t>(nt) * tn) * nR + i);
+            r.phi = unit_deriv32(E->phi, (static_cast<std::size_t>(tn) + static_cast<std::size_t>(nt) * ti) * nR + i);
+          }
+      E->dv.reserve(der.size());
+      FLY_CUDA(cudaMemcpy(E->dv.p, der.data(), der.size() * sizeof(DerRec), cudaMemcpyHostToDevice));
     }
     return E.release();
   }
