@@ -66,6 +66,9 @@ namespace flygpu {
     double shift[3];        // binary32 packed-coordinate offset per axis
     double rc_list;         // neighbour-list cut-off of this search
     double theta_tol_hist;  // collision angle (Master::find_batch, find.cpp:692)
+    // |x - in_min|^2 over the static atoms (fixed for the search): with the per-saddle sums stored after
+    // the history vectors it makes the device's mobile-DOF history check the reference's 3N one
+    double hist_static_on2;
     // this search's arrays (inside a batch's shared buffers or a served request's own block)
     D4* xl;                 // list positions per atom (w = F')
     Packed* pk;             // binary32 records per atom
@@ -74,7 +77,8 @@ namespace flygpu {
     std::uint16_t* ncnt;    // per atom
     std::uint16_t* nbr;     // [NB_CAP][n]
     double* vec;            // (N_VEC + 2 mT + 2 mR) vectors of 3 na doubles
-    double const* hist;     // n_hist vectors of 3 na doubles (previous saddle points)
+    double const* hist;     // n_hist vectors of 3 na doubles (previous saddle points), then per saddle h
+                            // sum (x - in_min).(sp_h - in_min) and |sp_h - in_min|^2 over static atoms
     std::uint8_t* mob;      // per atom: 1 if it can move (mobile), else 0
     double* rho0;           // per static atom: density from its static neighbours (fixed for the search)
     std::uint16_t* need;    // atoms whose F' the force pass reads (mobile atoms and their neighbours)

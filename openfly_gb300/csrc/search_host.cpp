@@ -229,7 +229,7 @@ namespace flygpu {
     int const mT = dimer ? o.mT : o.mL, mR = dimer ? o.mR : 0;
     S.na = na;
     S.count_frozen = count_frozen;
-    SearchLayout const l = search_layout(n, na, (N_VEC + 2 * mT + 2 * mR) * M, S.n_hist * M);
+    SearchLayout const l = search_layout(n, na, (N_VEC + 2 * mT + 2 * mR) * M, S.n_hist * (M + 2));
     if (img.size() < at + l.total) img.resize(at + l.total, 0);
     char* base = img.data() + at;
     D4* xl = reinterpret_cast<D4*>(base + l.xl);
@@ -254,6 +254,26 @@ namespace flygpu {
         v[V_INMIN * M + 3 * k + c] = in_min[3 * a + c];
         for (int hh = 0; hh < S.n_hist; ++hh)
           h[hh * M + 3 * k + c] = d.hist[static_cast<std::size_t>(hh) * 3 * static_cast<std::size_t>(n) + 3 * static_cast<std::size_t>(a) + static_cast<std::size_t>(c)];
+      }
+    }
+    // Dimer::find_sp's history check (dimer.cpp:102-131) dots x - in_min with sp - in_min over all 3n
+    // coordinates. Static atoms never move in a search, so their share of both dots and of |x - in_min|^2
+    // is a constant of the search (zero when the static atoms sit at in_min, as in Master's searches).
+    S.hist_static_on2 = 0;
+    if (S.n_hist > 0) {
+      double* hs = h + static_cast<std::size_t>(S.n_hist) * static_cast<std::size_t>(M);
+      for (int hh = 0; hh < S.n_hist; ++hh) hs[2 * hh] = hs[2 * hh + 1] = 0;
+      for (int i = 0; i < n; ++i) {
+        if (mb[i]) continue;
+        for (int c = 0; c < 3; ++c) {
+          double const d1 = d.pos[3 * i + c] - in_min[3 * i + c];
+          S.hist_static_on2 += d1 * d1;
+          for (int hh = 0; hh < S.n_hist; ++hh) {
+            double const d2 = d.hist[static_cast<std::size_t>(hh) * 3 * static_cast<std::size_t>(n) + 3 * static_cast<std::size_t>(i) + static_cast<std::size_t>(c)] - in_min[3 * i + c];
+            hs[2 * hh] += d1 * d2;
+            hs[2 * hh + 1] += d2 * d2;
+          }
+        }
       }
     }
     return l;

@@ -1599,9 +1599,11 @@ namespace flygpu {
                   q1 += d2 * d2;
                   q2 += d1 * d1;
                 }
-                q0 = warp_sum(q0);
-                q1 = warp_sum(q1);
-                q2 = warp_sum(q2);
+                // plus the static atoms' constant shares (the reference dots over all 3n coordinates)
+                double const* hs = c.hist + static_cast<std::int64_t>(S->n_hist) * M + 2 * h;
+                q0 = warp_sum(q0) + hs[0];
+                q1 = warp_sum(q1) + hs[1];
+                q2 = warp_sum(q2) + S->hist_static_on2;
                 double const ct = ctheta;
                 ctheta = lane0([&] { return fmax(ct, q0 / (sqrt(q1) * sqrt(q2))); });
                 double const cth = ctheta;
