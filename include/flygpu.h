@@ -151,6 +151,33 @@ int flygpu_eam_energy_gradient_noalloc(const flygpu_eam* eam, const double* d_po
                                        const uint8_t* d_frozen, int64_t n, const double extents[3],
                                        const int periodic[3], double* d_energy, double* d_grad, void* stream);
 
+/* ---------------------------------------------------------------- perturbations
+ * The random stream of Master (saddle/find.hpp:314): xoshiro256** 1.0 (utility/random.hpp:42-162),
+ * 256 bits of state. The reference seeds thread 0's generator from std::random_device and thread k's
+ * k long jumps further (find.cpp:188-193). These calls need no GPU. */
+typedef struct {
+  uint64_t s[4];
+} flygpu_xoshiro;
+/* Xoshiro::Xoshiro(seed) (random.hpp:72-76): an all-zero seed is rejected (FLYGPU_INVALID_ARG). */
+int flygpu_xoshiro_seed(flygpu_xoshiro* prng, const uint64_t seed[4]);
+/* Xoshiro::operator() (random.hpp:94-109) */
+uint64_t flygpu_xoshiro_next(flygpu_xoshiro* prng);
+/* Xoshiro::long_jump (random.hpp:130-132): 2^192 outputs ahead. */
+void flygpu_xoshiro_long_jump(flygpu_xoshiro* prng);
+/* count draws of one std::normal_distribution<double>(mean, stddev) object from prng, as libstdc++
+ * produces them (Marsaglia's polar method, the second value of each pair cached for the next draw).
+ * The draws Master::perturb makes come from three such objects (find.cpp:1152-1164). */
+int flygpu_normal_draws(flygpu_xoshiro* prng, double mean, double stddev, int64_t count, double* out);
+/* Master::perturb (saddle/find.cpp:1147-1214): out_pos = in_pos with Gaussian noise of a stddev drawn
+ * from N(stddev, stddev / 3) (redrawn while negative), scaled by 1 - r / r_pert, on every unfrozen
+ * neighbour of `centre` within r_pert in nl_pert's List::for_neighbours order, and unscaled on the
+ * centre; out_axis = Gaussian components on the same atoms, normalised over all 3n. nl_pert is a list
+ * of cut-off >= r_pert rebuilt on in_pos (find.cpp:217-219). Draws from prng in the reference's order;
+ * stddev_used (may be NULL) receives the stddev drawn. */
+int flygpu_perturb(flygpu_list* nl_pert, int64_t centre, const double* in_pos, const uint8_t* frozen, int64_t n,
+                   double stddev, double r_pert, flygpu_xoshiro* prng, double* out_pos, double* out_axis,
+                   double* stddev_used);
+
 /* ---------------------------------------------------------------- searches */
 
 /* Dimer::Options (saddle/dimer.hpp:56-98) then Rotor::Options (saddle/rotor.hpp:47-60). */

@@ -284,6 +284,29 @@ int flygpu_list_neighbours(flygpu_list* list, double r_cut, int32_t* counts, int
   });
 }
 
+int flygpu_perturb(flygpu_list* nl_pert, int64_t centre, const double* in_pos, const uint8_t* frozen, int64_t n,
+                   double stddev, double r_pert, flygpu_xoshiro* prng, double* out_pos, double* out_axis,
+                   double* stddev_used) {
+  return guard([&] {
+    need(nl_pert && in_pos && frozen && prng && out_pos && out_axis, "null argument");
+    need(n == nl_pert->n, "atom count differs from the list's");
+    need(centre >= 0 && centre < n, "centre out of range");
+    need(!frozen[centre], "perturbation centred on a frozen atom");  // find.cpp:1206
+    need(r_pert > 0 && stddev > 0, "r_pert and stddev must be positive");
+    std::vector<int> idx;
+    std::vector<double> dr;
+    int const c = list_neighbours_of(nl_pert, r_pert, centre, idx, dr);
+    check_device(nl_pert);
+    std::vector<double> r(static_cast<std::size_t>(c));
+    for (int k = 0; k < c; ++k) {
+      double const* d = &dr[3 * static_cast<std::size_t>(k)];
+      r[static_cast<std::size_t>(k)] = std::sqrt((d[0] * d[0] + d[1] * d[1]) + d[2] * d[2]);
+    }
+    double const s = perturb(idx, r, centre, in_pos, frozen, n, stddev, r_pert, *prng, out_pos, out_axis);
+    if (stddev_used) *stddev_used = s;
+  });
+}
+
 int flygpu_list_set_timing(flygpu_list* list, int enable) {
   return guard([&] {
     need(list, "null handle");

@@ -278,6 +278,10 @@ namespace flygpu {
   // the per-atom counts on the host. Synchronises the list's stream.
   std::vector<int> list_export_device(flygpu_list* L, double r_cut, DevBuf<long long>& offs, DevBuf<int>& idx,
                                       DevBuf<double>& dr);
+  // One real atom's neighbours within r_cut in List::for_neighbours order: real indices and binary64
+  // r_n - r_i (3 per entry). Synchronises the list's stream; returns the count.
+  int list_neighbours_of(flygpu_list* L, double r_cut, std::int64_t atom, std::vector<int>& idx,
+                         std::vector<double>& dr);
   // n_types bounds the type indices (out-of-range types raise FLYGPU_INVALID_ARG).
   void list_set_atoms(flygpu_list* L, int n_types, std::uint32_t const* d_types, std::uint8_t const* d_frozen,
                       bool copy_from_host, std::uint32_t const* h_types, std::uint8_t const* h_frozen);
@@ -309,6 +313,12 @@ namespace flygpu {
   // The same for a 3n x 3n Hessian whose frozen atoms' rows and columns are zero (only the active block
   // is diagonalised; one exact zero per frozen coordinate is merged in).
   void hessian_eigenvalues(flygpu_list* L, double* d_H, std::uint8_t const* h_frozen, double* h_eig);
+
+  // perturb.cpp: Master::perturb given the centre's neighbours (real indices and distances, in
+  // List::for_neighbours order); returns the stddev drawn.
+  double perturb(std::vector<int> const& nbr, std::vector<double> const& nbr_r, std::int64_t centre,
+                 double const* in_pos, std::uint8_t const* frozen, std::int64_t n, double stddev_opt, double r_pert,
+                 flygpu_xoshiro& g, double* out_pos, double* out_axis);
 
   // tables.cpp
   void build_spline(std::vector<double> y, double dx, double* out4, int n_spines);

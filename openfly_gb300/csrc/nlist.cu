@@ -343,6 +343,34 @@ namespace flygpu {
       counts[pimg[p]] = c;
     }
 
+    // The neighbours within r_cut of one real atom, in list order: real indices and r_n - r_i.
+    __global__ void k_export_one(D4 const* __restrict__ pos, int const* __restrict__ real_phys,
+                                 int const* __restrict__ pimg, int const* __restrict__ nbr,
+                                 int const* __restrict__ ncount, std::int64_t n, double rc2, std::int64_t atom, int cap,
+                                 int* __restrict__ idx, double* __restrict__ dr, int* __restrict__ count) {
+      std::int64_t const j = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+      if (j >= n) return;
+      int const p = real_phys[j];
+      if (pimg[p] != atom) return;
+      D4 const ri = pos[p];
+      int c = 0;
+      for (int k = 0; k < ncount[j]; ++k) {
+        int const q = nbr[static_cast<std::int64_t>(k) * n + j];
+        D4 const rq = pos[q];
+        double const dx = rq.x - ri.x, dy = rq.y - ri.y, dz = rq.z - ri.z;
+        if ((dx * dx + dy * dy) + dz * dz < rc2) {
+          if (c < cap) {
+            idx[c] = pimg[q];
+            dr[3 * c + 0] = dx;
+            dr[3 * c + 1] = dy;
+            dr[3 * c + 2] = dz;
+          }
+          ++c;
+        }
+      }
+      *count = c;
+    }
+
     __global__ void k_export_fill(D4 const* __restrict__ pos, int const* __restrict__ real_phys,
                                   int const* __restrict__ pimg, int const* __restrict__ nbr,
                                   int const* __restrict__ ncount, std::int64_t n, double rc2,
@@ -614,6 +642,34 @@ namespace flygpu {
       FLY_CUDA(cudaStreamSynchronize(s));
     }
     return total;
+  }
+
+  int list_neighbours_of(flygpu_list* L, double r_cut, std::int64_t atom, std::vector<int>& idx,
+                         std::vector<double>& dr) {
+    if (!L->built) fail(FLYGPU_INVALID_ARG, "neighbours() before rebuild()");
+    if (r_cut > L->g.rc) fail(FLYGPU_INVALID_ARG, "r_cut is bigger than the list's cut-off");
+    if (atom < 0 || atom >= L->n) fail(FLYGPU_INVALID_ARG, "atom index out of range");
+    cudaStream_t const s = L->stream;
+    int const cap = std::max(1, L->nb_cap);
+    DevBuf<int> d_idx, d_cnt;
+    DevBuf<double> d_dr;
+    d_idx.reserve(static_cast<std::size_t>(cap));
+    d_cnt.reserve(1);
+    d_dr.reserve(3 * static_cast<std::size_t>(cap));
+    launch(k_export_one, blocks_for(L->n), T, 0, s, L->pos.p, L->real_phys.p, L->pimg.p, L->nbr.p, L->ncount.p, L->n,
+           r_cut * r_cut, atom, cap, d_idx.p, d_dr.p, d_cnt.p);
+    int c = 0;
+    FLY_CUDA(cudaMemcpyAsync(&c, d_cnt.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    FLY_CUDA(cudaStreamSynchronize(s));
+    c = std::min(c, cap);
+    idx.resize(static_cast<std::size_t>(c));
+    dr.resize(3 * static_cast<std::size_t>(c));
+    if (c > 0) {
+      FLY_CUDA(cudaMemcpyAsync(idx.data(), d_idx.p, sizeof(int) * idx.size(), cudaMemcpyDeviceToHost, s));
+      FLY_CUDA(cudaMemcpyAsync(dr.data(), d_dr.p, sizeof(double) * dr.size(), cudaMemcpyDeviceToHost, s));
+      FLY_CUDA(cudaStreamSynchronize(s));
+    }
+    return c;
   }
 
   std::vector<int> list_export_device(flygpu_list* L, double r_cut, DevBuf<long long>& offs, DevBuf<int>& idx,

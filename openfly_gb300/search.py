@@ -6,6 +6,9 @@
                                 saddle/find.cpp:684-732)
   search_plain                  one search the drop-in way: host search loop, GPU List + EAM
   Server                        continuous batching of searches (openfly_gb300.serve)
+  Xoshiro / perturb             Master's random stream and Master::perturb (find.cpp:1147-1214)
+  find_batch                    Master::find_batch (find.cpp:684-755): perturb, batched searches with the
+                                saddle cache as history, retries on Spline::OutOfBounds, mechanisms, caching
 """
 from __future__ import annotations
 
@@ -105,6 +108,12 @@ def _setup() -> None:
     L.flygpu_batch_device_bytes.restype = C.c_int64
     L.flygpu_batch_device_bytes.argtypes = [V]
     L.flygpu_search_plain.argtypes = [V, V, V, C.c_int, V, V, V, V]
+    L.flygpu_xoshiro_seed.argtypes = [V, V]
+    L.flygpu_xoshiro_next.restype = C.c_uint64
+    L.flygpu_xoshiro_next.argtypes = [V]
+    L.flygpu_xoshiro_long_jump.argtypes = [V]
+    L.flygpu_normal_draws.argtypes = [V, C.c_double, C.c_double, C.c_int64, V]
+    L.flygpu_perturb.argtypes = [V, C.c_int64, V, V, C.c_int64, C.c_double, C.c_double, V, V, V, V]
     _ready = True
 
 
@@ -310,14 +319,149 @@ class Server:
 
 
 def centroid(x: np.ndarray) -> np.ndarray:
-    """utility/lattice.hpp:203-209: the mean position."""
-    return np.asarray(x, np.float64).reshape(-1, 3).mean(axis=0)
+    """utility/lattice.hpp:203-209: the mean position (a sequential sum over atoms, then / N)."""
+    x = np.asarray(x, np.float64).reshape(-1, 3)
+    return np.cumsum(x, axis=0)[-1] / x.shape[0]
 
 
 def centroid_align(x: np.ndarray, with_: np.ndarray) -> np.ndarray:
     """utility/lattice.hpp:214-226: x translated so that its centroid is the centroid of ``with_``."""
     x = np.asarray(x, np.float64).reshape(-1, 3)
     return x + (centroid(with_) - centroid(x))
+
+
+class XoshiroState(C.Structure):
+    _fields_ = [("s", C.c_uint64 * 4)]
+
+
+class Xoshiro:
+    """Master's random stream (saddle/find.hpp:314): xoshiro256** 1.0 (utility/random.hpp:42-162) through
+    flygpu_xoshiro_*. Host only; needs no GPU."""
+
+    def __init__(self, seed):
+        _setup()
+        self.st = XoshiroState()
+        check(lib().flygpu_xoshiro_seed(C.byref(self.st), (C.c_uint64 * 4)(*[int(x) for x in seed])), "Xoshiro")
+
+    @property
+    def state(self) -> tuple:
+        return tuple(int(x) for x in self.st.s)
+
+    def copy(self) -> "Xoshiro":
+        return Xoshiro(self.state)
+
+    def assign(self, other: "Xoshiro") -> None:
+        for k in range(4):
+            self.st.s[k] = other.st.s[k]
+
+    def next(self) -> int:
+        return int(lib().flygpu_xoshiro_next(C.byref(self.st)))
+
+    def long_jump(self) -> None:
+        lib().flygpu_xoshiro_long_jump(C.byref(self.st))
+
+    def normal(self, mean: float, stddev: float, count: int) -> np.ndarray:
+        """count draws of one std::normal_distribution<double>(mean, stddev) object (libstdc++'s)."""
+        out = np.zeros(count)
+        check(lib().flygpu_normal_draws(C.byref(self.st), mean, stddev, count, out.ctypes.data), "normal")
+        return out
+
+
+def perturb(nl_pert, centre: int, in_pos, frozen, prng: Xoshiro, stddev: float = 0.6, r_pert: float = 4.0):
+    """Master::perturb (find.cpp:1147-1214) through flygpu_perturb: nl_pert is a List of cut-off >= r_pert
+    rebuilt on in_pos. Returns (positions (n,3), unit axis (n,3), stddev drawn); advances prng."""
+    _setup()
+    x = np.ascontiguousarray(in_pos, dtype=np.float64).reshape(-1)
+    fz = np.ascontiguousarray(frozen, dtype=np.uint8)
+    n = x.size // 3
+    out, ax = np.zeros(3 * n), np.zeros(3 * n)
+    sd = C.c_double()
+    check(lib().flygpu_perturb(nl_pert.h, int(centre), x.ctypes.data, fz.ctypes.data, n, stddev, r_pert,
+                               C.byref(prng.st), out.ctypes.data, ax.ctypes.data, C.byref(sd)), "perturb")
+    return out.reshape(-1, 3), ax.reshape(-1, 3), sd.value
+
+
+def theta_tol(tot: int) -> float:
+    """Master::find_batch's collision angle after `tot` searches around one centre (find.cpp:692)."""
+    return ((30 - 2.5) * np.exp(-0.02 * tot) + 2.5) / 360.0 * 2.0 * np.pi
+
+
+def find_batch(eam: EAM, tot: int, minimum: Search, centre: int, nl_pert, cache: list, batch_size: int,
+               prng: Xoshiro, geo, opts: "MasterOptions | None" = None, precision: int = MIXED,
+               dimer: DimerOptions | None = None, lbfgs: LBFGSOptions | None = None, masses=None,
+               zero_modes: int | None = None, tuning: Tuning | None = None, max_retries: int = 3) -> list:
+    """Master::find_batch (find.cpp:684-755) over one batched launch.
+
+    For each of batch_size searches: perturb the minimum around `centre` (`perturb`, drawing from prng),
+    centroid_align onto the minimum when no atom is frozen, then run every search in one Batch with the
+    saddle cache as history and the collision angle theta_tol(tot) (find_sp, find.cpp:983-1009). A search
+    that ends in Spline::OutOfBounds is perturbed again and rerun, and after max_retries retries a
+    RuntimeError is raised (find.cpp:706-722). The draws are those of the reference run on one thread: a
+    retry's perturbation is drawn right after the failed one, so when search k needs one, the searches
+    after k are perturbed again from that point of the stream and rerun with it. Each successful saddle
+    goes through saddle_2_mech (`mechanisms`, geometry `geo`); a success that yields no mechanism is
+    appended to cache, as the reference caches it for later collision checks (find.cpp:734-745); failed
+    searches are not cached. zero_modes is the minimum's zero-mode count (None: computed from its Hessian,
+    `minimum_modes`). The catalogue step that follows (add_mech) is the caller's.
+
+    Returns one dict per search: exit_code, result (the search's result dict), pos, axis (final), start
+    (perturbed positions and axis of the attempt that ran), retries, mech (None or the mechanism)."""
+    from . import SPLINE_OOB
+
+    opts = opts or MasterOptions()
+    dimer = dimer or DimerOptions.defaults()
+    x0 = np.asarray(minimum.pos, np.float64).reshape(-1, 3)
+    frozen = np.asarray(minimum.frozen, np.uint8)
+    nothing_frozen = int(frozen.sum()) == 0
+    hist = [np.asarray(h, np.float64).reshape(-1, 3) for h in cache] or None
+    tt = theta_tol(tot)
+    starts: list = [None] * batch_size
+    out: list = [None] * batch_size
+    retries = [0] * batch_size
+    after = [None] * batch_size  # the stream's state after each search's latest perturbation
+    g, first = prng.copy(), 0
+    while first < batch_size:
+        for j in range(first, batch_size):
+            p, a, _ = perturb(nl_pert, centre, x0, frozen, g, opts.stddev, opts.r_pert)
+            if nothing_frozen:
+                p = centroid_align(p, x0)
+            starts[j] = (p, a)
+            after[j] = g.copy()
+        run = list(range(first, batch_size))
+        b = Batch(eam, [Search(starts[j][0], minimum.types, frozen, minimum.extents, minimum.periodic,
+                               axis=starts[j][1], in_min=x0, hist=hist, theta_tol=tt) for j in run],
+                  precision=precision, dimer=dimer, lbfgs=lbfgs)
+        b.run(tuning)
+        res, pos, ax = b.results()
+        for k, j in enumerate(run):
+            out[j] = (res[k], pos[k], ax[k])
+        oob = [j for j in run if out[j][0]["status"] == SPLINE_OOB]
+        bad = [j for j in run if out[j][0]["status"] not in (0, SPLINE_OOB)]
+        if bad:
+            check(out[bad[0]][0]["status"], f"find_batch search {bad[0]}")
+        if not oob:
+            break
+        j = oob[0]
+        retries[j] += 1
+        if retries[j] > max_retries:
+            raise RuntimeError(f"Consecutive spline-out-of-bounds @{centre}")
+        g, first = after[j].copy(), j
+    prng.assign(g)
+    succ = [j for j in range(batch_size) if out[j][0]["exit_code"] == EXIT_SUCCESS]
+    mechs: list = [None] * batch_size
+    if succ:
+        ms = mechanisms(eam, [Search(out[j][1], minimum.types, frozen, minimum.extents, minimum.periodic,
+                                     axis=out[j][2]) for j in succ],
+                        [x0] * len(succ), [np.asarray(geo)] * len(succ), masses=masses, opts=opts, precision=precision,
+                        dimer=dimer, lbfgs=lbfgs, zero_modes=None if zero_modes is None else [zero_modes] * len(succ),
+                        tuning=tuning)
+        for j, m in zip(succ, ms):
+            mechs[j] = m
+    for j in succ:
+        if mechs[j] is None:
+            cache.append(out[j][1].copy())
+    return [dict(exit_code=out[j][0]["exit_code"], result=out[j][0], pos=out[j][1], axis=out[j][2], start=starts[j],
+                 retries=retries[j], mech=mechs[j]) for j in range(batch_size)]
 
 
 def furthest_atom(pos: np.ndarray, extents, periodic, i: int) -> int:
@@ -450,7 +594,10 @@ class MasterOptions:
     defaults."""
 
     def __init__(self, basin_tol: float = 0.05, stationary_tol: float | None = None, capture_r_tol: float = 0.05,
-                 capture_E_tol: float = 0.01, hessian_eigen_zero_tol: float = 1e-6, nudge_frac: float = 0.01):
+                 capture_E_tol: float = 0.01, hessian_eigen_zero_tol: float = 1e-6, nudge_frac: float = 0.01,
+                 r_pert: float = 4.0, stddev: float = 0.6):
+        self.r_pert = r_pert  # find.hpp:97
+        self.stddev = stddev  # find.hpp:101
         self.basin_tol = basin_tol
         self.stationary_tol = basin_tol / 2 if stationary_tol is None else stationary_tol
         self.capture_r_tol = capture_r_tol

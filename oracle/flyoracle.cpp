@@ -17,6 +17,8 @@
 //   src/saddle/rotor.cpp:33-164                                       (trans_proj, Rotor::eff_gradient)
 //   src/saddle/dimer.cpp:28-171                                       (Dimer::find_sp)
 //   utility/random.hpp:42-162                                         (Xoshiro256**)
+//   src/saddle/find.cpp:1147-1214                                     (Master::perturb, with libstdc++'s
+//                                                                      std::normal_distribution as the reference uses it)
 //   utility/core.hpp:539-542,634-680                                  (near, gdot, gnorm)
 //
 // Arithmetic conventions (fixed here so the oracle is deterministic on x86-64 and aarch64):
@@ -38,6 +40,7 @@
 #include <fstream>
 #include <limits>
 #include <memory>
+#include <random>
 #include <sstream>
 #include <stdexcept>
 #include <string>
@@ -823,7 +826,12 @@ namespace orc {
 
   // ---------------------------------------------------------------- Xoshiro256** (random.hpp:42-162)
 
+  // A UniformRandomBitGenerator (random.hpp:42-162), so std::normal_distribution draws from it exactly
+  // as the reference's Master::perturb does (find.cpp:1150-1164).
   struct Xoshiro {
+    using result_type = std::uint64_t;
+    static constexpr result_type min() { return 0; }
+    static constexpr result_type max() { return std::numeric_limits<result_type>::max(); }
     std::uint64_t s[4];
     static std::uint64_t rotl(std::uint64_t x, int k) { return (x << k) | (x >> (64 - k)); }
     std::uint64_t operator()() {
@@ -1190,6 +1198,49 @@ int orc_dimer_batch(void* h, orc_dimer_options const* opt, int n_search, long co
 void orc_xoshiro(std::uint64_t const* seed, std::uint64_t* out, long n) {
   orc::Xoshiro g{{seed[0], seed[1], seed[2], seed[3]}};
   for (long i = 0; i < n; ++i) out[i] = g();
+}
+
+// count draws of one libstdc++ std::normal_distribution<double>(mean, stddev) from the stream seeded by
+// state (updated in place).
+void orc_normal_draws(std::uint64_t* state, double mean, double stddev, long count, double* out) {
+  orc::Xoshiro g{{state[0], state[1], state[2], state[3]}};
+  std::normal_distribution<double> d(mean, stddev);
+  for (long i = 0; i < count; ++i) out[i] = d(g);
+  std::memcpy(state, g.s, sizeof g.s);
+}
+
+// Master::perturb (src/saddle/find.cpp:1147-1214) with the oracle's List (built with cut-off r_pert on
+// in_pos, find.cpp:217-219): the stddev prime draws, then per unfrozen neighbour of the centre in
+// for_neighbours order three position draws (scaled by 1 - r / r_pert) and three axis draws, then the
+// centre's, the axis normalised over all 3n (sequential sum). state is updated in place.
+int orc_perturb(void* l, long centre, double const* in_pos, std::uint8_t const* frozen, long n, double stddev_opt,
+                double r_pert, std::uint64_t* state, double* out_pos, double* out_axis, double* stddev_used) {
+  return guarded([&] {
+    auto const& nl = *static_cast<orc::List*>(l);
+    orc::Xoshiro prng{{state[0], state[1], state[2], state[3]}};
+    std::normal_distribution<double> normal(0., 1.);
+    std::normal_distribution<double> prime(stddev_opt, stddev_opt / 3.0);
+    double stddev = -1;
+    while (stddev < 0) stddev = prime(prng);
+    std::normal_distribution<double> gauss(0, stddev);
+    std::memcpy(out_pos, in_pos, sizeof(double) * 3 * static_cast<std::size_t>(n));
+    std::fill_n(out_axis, 3 * n, 0.0);
+    nl.for_neighbours(centre, r_pert, [&](long a, double r, double const*) {
+      if (!frozen[a]) {
+        double const env = 1. - r / r_pert;
+        for (int k = 0; k < 3; ++k) out_pos[3 * a + k] += gauss(prng) * env;
+        for (int k = 0; k < 3; ++k) out_axis[3 * a + k] += normal(prng);
+      }
+    });
+    for (int k = 0; k < 3; ++k) out_pos[3 * centre + k] += gauss(prng);
+    for (int k = 0; k < 3; ++k) out_axis[3 * centre + k] += normal(prng);
+    double ss = 0;
+    for (long k = 0; k < 3 * n; ++k) ss += out_axis[k] * out_axis[k];
+    double const nrm = std::sqrt(ss);
+    for (long k = 0; k < 3 * n; ++k) out_axis[k] /= nrm;
+    *stddev_used = stddev;
+    std::memcpy(state, prng.s, sizeof prng.s);
+  });
 }
 
 int orc_max_threads() { return omp_get_max_threads(); }

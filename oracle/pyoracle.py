@@ -81,6 +81,7 @@ _lp = np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS")
 _up = np.ctypeslib.ndpointer(dtype=np.uint32, flags="C_CONTIGUOUS")
 _bp = np.ctypeslib.ndpointer(dtype=np.uint8, flags="C_CONTIGUOUS")
 _u64p = np.ctypeslib.ndpointer(dtype=np.uint64, flags="C_CONTIGUOUS")
+_u8p = np.ctypeslib.ndpointer(dtype=np.uint8, flags="C_CONTIGUOUS")
 
 _lib = None
 
@@ -134,6 +135,9 @@ def lib() -> C.CDLL:
         L.orc_dimer_batch.argtypes = [V, C.POINTER(DimerOptions), C.c_int, _lp, _dp, _ip, _dp, _dp, _up, _bp, _ip,
                                       C.c_int, _ip, _ip]
         L.orc_xoshiro.argtypes = [_u64p, _u64p, C.c_long]
+        L.orc_normal_draws.argtypes = [_u64p, C.c_double, C.c_double, C.c_long, _dp]
+        L.orc_perturb.argtypes = [C.c_void_p, C.c_long, _dp, _u8p, C.c_long, C.c_double, C.c_double, _u64p, _dp,
+                                  _dp, C.POINTER(C.c_double)]
         L.orc_max_threads.restype = C.c_int
         L.orc_adjacent.argtypes = [_ip, C.c_int, _ip]
         L.orc_cell_idx.argtypes = [_dp, C.c_double, _dp]
@@ -144,6 +148,70 @@ def lib() -> C.CDLL:
 def _check(st: int, what: str) -> None:
     if st != OK:
         raise OracleError(st, what)
+
+
+def normal_draws(state, mean: float, stddev: float, count: int):
+    """count draws of std::normal_distribution<double>(mean, stddev) (libstdc++) from the xoshiro256**
+    stream in state; returns (draws, state after)."""
+    st = np.array(state, dtype=np.uint64)
+    out = np.zeros(count, dtype=np.float64)
+    lib().orc_normal_draws(st, mean, stddev, count, out)
+    return out, st
+
+
+def perturb(nl: "List", centre: int, in_pos, frozen, stddev: float, r_pert: float, state):
+    """Master::perturb (find.cpp:1147-1214) with nl built with cut-off r_pert on in_pos; returns
+    (positions (n,3), axis (n,3), stddev drawn, state after)."""
+    x = np.ascontiguousarray(in_pos, dtype=np.float64).reshape(-1)
+    n = x.size // 3
+    out, ax = np.zeros(3 * n), np.zeros(3 * n)
+    st = np.array(state, dtype=np.uint64)
+    sd = C.c_double()
+    _check(lib().orc_perturb(nl.h, centre, x, np.ascontiguousarray(frozen, dtype=np.uint8), n, stddev, r_pert, st,
+                             out, ax, C.byref(sd)), "perturb")
+    return out.reshape(-1, 3), ax.reshape(-1, 3), sd.value, st
+
+
+def find_batch(data: EAMData, dimer_opt: DimerOptions, lbfgs_opt: LBFGSOptions, tot: int, extents, periodic,
+               in_pos, types, frozen, centre: int, nl_pert: "List", cache: list, batch_size: int, state, geo,
+               masses, zero_modes: int, stddev: float = 0.6, r_pert: float = 4.0, max_retries: int = 3):
+    """Master::find_batch (saddle/find.cpp:684-755) run on one thread: per search, perturb (:707) and
+    centroid_align when nothing is frozen (:709-711), Dimer::find_sp with the cache as history and the
+    collision angle of :692 (find_sp, :983-1009), retried with a new perturbation on Spline::OutOfBounds
+    up to max_retries times before raising (:712-721); saddle_2_mech on a success (:725-729); after the
+    batch, a success without a mechanism is cached (:734-745). Returns (per-search dicts, state after)."""
+    theta_tol = ((30 - 2.5) * np.exp(-0.02 * tot) + 2.5) / 360.0 * 2.0 * np.pi
+    x0 = np.asarray(in_pos, np.float64).reshape(-1, 3)
+    fz = np.asarray(frozen, np.uint8)
+    nothing_frozen = int(fz.sum()) == 0
+    hist = [np.asarray(h, np.float64).reshape(-1, 3) for h in cache]
+    out = []
+    for _ in range(batch_size):
+        retry = 0
+        while True:
+            p, a, _, state = perturb(nl_pert, centre, x0, fz, stddev, r_pert, state)
+            if nothing_frozen:
+                p = p + (np.cumsum(x0, axis=0)[-1] / x0.shape[0] - np.cumsum(p, axis=0)[-1] / p.shape[0])
+            try:
+                r = dimer_find_sp(data, dimer_opt, extents, periodic, p, a, types, fz, in_min=x0, hist=hist or None,
+                                  theta_tol=theta_tol)
+                break
+            except OracleError as e:
+                if e.status != SPLINE_OOB:
+                    raise
+                retry += 1
+                if retry > max_retries:
+                    raise RuntimeError(f"Consecutive spline-out-of-bounds @{centre}")
+        mech = None
+        if r["exit"] == 0:
+            mech = mechanism(data, dimer_opt, lbfgs_opt, extents, periodic, types, fz, x0, r["x"], r["axis"], geo,
+                             masses, zero_modes)
+        out.append(dict(exit=r["exit"], steps=r["steps"], x=r["x"], axis=r["axis"], start=(p, a), retries=retry,
+                        mech=mech))
+    for o in out:
+        if o["mech"] is None and o["exit"] == 0:
+            cache.append(o["x"].copy())
+    return out, state
 
 
 def xoshiro(seed, n: int) -> np.ndarray:
