@@ -57,9 +57,15 @@ def make_workload(cells: int):
     return s, fields
 
 
-def schedule(steps: int):
-    """(field index, sign, rebuild-after-update?) per step, with the reference's skin rule."""
-    acc, out = 0.0, []
+# Accumulated displacement at the start of a timed window: the window's 16th step triggers the first
+# rebuild and every 31st after it, so any window of 16 or more steps holds at least its share of rebuilds.
+ACC_TIMED = 0.5 * SKIN - 15 * STEP_DISP
+
+
+def schedule(steps: int, acc0: float = 0.0):
+    """(field index, sign, rebuild-after-update?) per step, with the reference's skin rule, starting from an
+    accumulated displacement acc0."""
+    acc, out = acc0, []
     for k in range(steps):
         j, sign = (k // 2) % N_FIELDS, (1.0 if k % 2 == 0 else -1.0)
         acc += STEP_DISP
@@ -143,8 +149,8 @@ def measured_peak_hbm() -> tuple[float, str]:
 
 def traffic_from_profile(kernel: str, atoms: int) -> float | None:
     """DRAM bytes (read + write) of one launch of `kernel` at `atoms` atoms, from the committed ncu
-    capture of a smaller case (profiles/eam_passes_fe_h_crystal_split_records.md), scaled by atom count: the traffic of a
-    pass grows in proportion to the atoms it processes."""
+    capture of a smaller Fe-H crystal (profiles/fe_h_crystal_dram_traffic.json), scaled by atom count: the
+    traffic of a pass grows in proportion to the atoms it processes."""
     p = os.path.join(ROOT, "profiles", "fe_h_crystal_dram_traffic.json")
     if os.path.exists(p):
         k = json.load(open(p)).get(kernel)
@@ -155,7 +161,7 @@ def traffic_from_profile(kernel: str, atoms: int) -> float | None:
 
 # ----------------------------------------------------------------------------- CPU (oracle) leg
 
-def cpu_crystal_steps(s, fields, steps: int, threads: int):
+def cpu_crystal_steps(s, fields, steps: int, threads: int, acc0: float = ACC_TIMED):
     """The reference's CPU path (oracle port) on the same steps; returns (seconds, steps, rebuilds)."""
     from oracle import pyoracle as O
     from openfly_gb300 import workloads as W
@@ -163,7 +169,7 @@ def cpu_crystal_steps(s, fields, steps: int, threads: int):
     data = O.EAMData(W.TABLE)
     nl = O.List(s.extents, s.periodic, data.r_cut + SKIN)
     nl.rebuild(s.pos, threads)
-    sched = schedule(steps)
+    sched = schedule(steps, acc0)
     pos_alt = [s.pos - f for f in fields]
     t0 = time.perf_counter()
     rebuilds = 0
@@ -295,9 +301,23 @@ def search_metrics(fly, args) -> dict:
             best = dt if best is None else min(best, dt)
         runs[name] = res
         pos_final[name] = b.results(positions=True)[1]  # untimed: final configurations for the same-saddle test
+        del b
+        # end to end: the batch built from the host descriptions (packing and upload), run and read back
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        b2 = S.Batch(eam, reqs, precision=prec, dimer=opt)
+        b2.run(tune)
+        res2, _, _ = b2.results(positions=True)
+        e2e_s = time.perf_counter() - t0
+        del b2
         ex = [r["exit_code"] for r in res]
         out["batched"][name] = {"searches_per_s": len(reqs) / best, "seconds": best, "tuning": tune.as_dict(),
                                 "converged": ex.count(0), "convex": ex.count(-1), "iter_max": ex.count(-2),
+                                "saddles_per_s": ex.count(0) / best,
+                                "e2e": {"searches_per_s": len(reqs) / e2e_s, "seconds": e2e_s,
+                                        "saddles_per_s": sum(r["exit_code"] == 0 for r in res2) / e2e_s,
+                                        "note": "flygpu_batch_create (host packing + upload) + run + results with "
+                                                "final positions and axes, timed together"},
                                 "errors": sum(r["status"] != 0 for r in res),
                                 "grad_calls_mean": float(np.mean([r["grad_calls"] for r in res]))}
     # Both precisions converged and ended on the same saddle (every atom within SAME_SADDLE_A): the
@@ -339,6 +359,51 @@ def search_metrics(fly, args) -> dict:
     out["served"]["saturated"] = serve_run(S, eam, stream, tune, opt, args, None)
     out["mechanisms"] = mechanism_metrics(fly, eam, S, W)
     out["gpu_launches"] = int(fly.launch_count() - l0)
+    # kept for the CPU leg's comparison with the oracle (not printed)
+    out["_oracle_sample"] = (clusters[:ORACLE_SAMPLE], {k: v[:ORACLE_SAMPLE] for k, v in runs.items()},
+                             {k: v[:ORACLE_SAMPLE] for k, v in pos_final.items()})
+    return out
+
+
+ORACLE_SAMPLE = 96  # batched searches also run by the oracle in the CPU leg
+
+
+def oracle_search_agreement(sample, threads: int) -> dict:
+    """The first ORACLE_SAMPLE batched searches against the oracle's Dimer::find_sp on the same inputs:
+    the fraction with the reference's exit code, the fraction of jointly converged pairs on the same saddle
+    (every atom within SAME_SADDLE_A) and their saddle-energy differences, per precision."""
+    from oracle import pyoracle as O
+    from openfly_gb300 import workloads as W
+
+    clusters, runs, pos = sample
+    od = O.EAMData(W.TABLE)
+    oopt = O.DimerOptions.defaults(n=6, rot_n=6, f2norm=1e-3, max_steps=1000)
+    sys_ = [c.sys for c in clusters]
+    offs = np.concatenate([[0], np.cumsum([x.n for x in sys_])]).astype(np.int64)
+    t0 = time.perf_counter()
+    ex, st, x, _ = O.dimer_batch(od, oopt, offs, np.stack([x.extents for x in sys_]), np.stack([x.periodic for x in sys_]),
+                                 np.concatenate([x.pos for x in sys_]), np.concatenate([c.axis for c in clusters]),
+                                 np.concatenate([x.types for x in sys_]), np.concatenate([x.frozen for x in sys_]),
+                                 np.array([int(x.frozen.sum()) for x in sys_], np.int32), threads)
+    secs = time.perf_counter() - t0
+    out = {"searches": len(clusters), "oracle_seconds": secs, "oracle_threads": threads, "same_saddle_A": SAME_SADDLE_A}
+    for name in runs:
+        same_exit = [int(r["exit_code"]) == int(e) for r, e in zip(runs[name], ex)]
+        both = [k for k, (r, e) in enumerate(zip(runs[name], ex)) if r["exit_code"] == 0 and e == 0]
+        same = []
+        for k in both:
+            xo = x[offs[k]:offs[k + 1]]
+            if np.abs(pos[name][k] - xo).max() < SAME_SADDLE_A:
+                same.append(k)
+        errs = []
+        for k in same:
+            s = sys_[k]
+            nl = O.List(s.extents, s.periodic, od.r_cut)
+            nl.rebuild(x[offs[k]:offs[k + 1]], 1)
+            errs.append(abs(runs[name][k]["energy"] - O.eam_energy(od, nl, s.types)) * 1e3)
+        out[name] = {"same_exit_fraction": float(np.mean(same_exit)), "both_converged": len(both),
+                     "same_saddle_fraction": len(same) / len(both) if both else None,
+                     "saddle_energy_err_meV_max": float(max(errs)) if errs else None}
     return out
 
 
@@ -450,7 +515,7 @@ def ours(args):
     for j, sign, rb in schedule(args.warmup):
         step(j, sign, rb)
     nl.sync()
-    sched = schedule(args.steps)
+    sched = schedule(args.steps, ACC_TIMED)
     if dist:
         tdist.barrier()
     torch.cuda.synchronize()
@@ -511,7 +576,7 @@ def ours(args):
     nl.rebuild_device(d_pos0, n)
     for j, sign, rb in schedule(args.warmup):
         step64(j, sign, rb)
-    sched64 = schedule(min(args.steps, 20))
+    sched64 = schedule(min(args.steps, 40), ACC_TIMED)
     torch.cuda.synchronize()
     ev2, ev3 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     ev2.record(stream)
@@ -520,9 +585,28 @@ def ours(args):
     ev3.record(stream)
     torch.cuda.synchronize()
     ms64 = reduce_max(ev2.elapsed_time(ev3), dev)
+
+    def step64_host(j, sign, rb):
+        if rb:
+            nl.rebuild((h_pos_alt[j] if sign > 0 else h_pos0).numpy())
+        else:
+            nl.update((h_fields[j] if sign > 0 else h_neg[j]).numpy())
+        return eam.energy_gradient(None, None, nl, fly.FP64, out=h_grad.numpy())[0]
+
+    nl.rebuild(h_pos0.numpy())
+    for j, sign, rb in schedule(args.warmup):
+        step64_host(j, sign, rb)
+    t0 = time.perf_counter()
+    for j, sign, rb in sched64:
+        step64_host(j, sign, rb)
+    e2e64_s = reduce_max(time.perf_counter() - t0, dev)
     fp64_line = {"value": replica_value(n, world, len(sched64), ms64), "unit": "atom-evals/s",
                  "steps": len(sched64), "ms_per_step": ms64 / len(sched64),
-                 "note": "binary64 EAM in the reference's operation order (bit-identical to the oracle)"}
+                 "rebuilds": sum(1 for *_, rb in sched64 if rb),
+                 "e2e": {"value": n * world * len(sched64) / e2e64_s, "unit": "atom-evals/s",
+                         "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+                 "note": "binary64 EAM in the reference's operation order (bit-identical to the oracle); e2e through "
+                         "the host C ABI with pinned buffers, as the headline's e2e"}
 
     # catalogue local environments (geometry + fingerprint of every atom) from the same list
     from openfly_gb300 import env as E
@@ -570,6 +654,7 @@ def ours(args):
                      "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
                      "algorithmic_bytes_per_atom": per_atom},
         "kernel_ms_per_step": {k: v[0] / max(1, args.steps) for k, v in ktimes.items()},
+        "rebuilds_in_window": n_rb,
         "step_algorithmic_GBps": ALGO_BYTES_STEP * n * args.steps / (ms * 1e-3) / 1e9,
         "gpu_launches": int(launches),
         "clocks": clk,
@@ -589,6 +674,9 @@ def ours(args):
                                 "sample": f"{k} steps ({rb} rebuild) of the same {n}-atom workload, oracle port, "
                                           f"{threads} OpenMP threads"}
         line["parity"] = parity_block(s, par, threads)
+        if "searches" in line:
+            line["searches"]["batched"]["vs_oracle"] = oracle_search_agreement(line["searches"].pop("_oracle_sample"),
+                                                                               threads)
         from oracle import pyoracle as O
 
         olmin = O.LBFGSOptions.defaults(iter_max=3, f2norm=1e-9)
@@ -616,6 +704,8 @@ def ours(args):
                                                    "and, separately, of the active block")
 
     if rank == 0:
+        if "searches" in line:
+            line["searches"].pop("_oracle_sample", None)
         print(json.dumps(line), flush=True)
     if dist:
         tdist.destroy_process_group()
@@ -694,67 +784,6 @@ def hessian_prefactor(fly, eam, reps: int = 5) -> dict:
             "note": "flygpu_hessian_eigenvalues: binary64 Hessian (bit-exact), mass weighting, cuSOLVER syevd of the active block"}
 
 
-def search_batch(args) -> None:
-    """One batched launch over --search-batch search clusters (lanes 2, 128 threads, 2 CTAs/SM), for
-    profiling the search kernel on a small case; prints one JSON line (not a bench line)."""
-    import openfly_gb300 as fly
-    from openfly_gb300 import search as S
-    from openfly_gb300 import workloads as W
-    from openfly_gb300.build import build
-
-    build()
-    eam = fly.EAM(W.TABLE)
-    opt = S.DimerOptions.defaults(n=6, rot_n=6, f2norm=1e-3, max_steps=args.max_search_steps)
-    prec = fly.MIXED if args.precision == "mixed" else fly.FP64
-    b = S.Batch(eam, [S.from_cluster(c) for c in W.search_clusters(n=args.search_batch, seed=7)], precision=prec, dimer=opt)
-    t0 = time.perf_counter()
-    b.run(S.Tuning(2, 128, 2, 0))
-    res, _, _ = b.results(positions=False)
-    dt = time.perf_counter() - t0
-    print(json.dumps({"search_batch": len(res), "precision": args.precision, "seconds": dt,
-                      "grad_calls": int(sum(r["grad_calls"] for r in res)),
-                      "errors": int(sum(r["status"] != 0 for r in res))}), flush=True)
-
-
-def search_tail(args) -> None:
-    """The tail of a batch of search clusters as one launch, for profiling: the batch of --searches clusters runs
-    once (8 lanes, 256 threads, 2 CTAs/SM, 128-register variant, one phase); the searches that needed more
-    than 100 translation steps then run alone in the wide shape (4 lanes, 256 threads, 1 CTA/SM). Prints
-    one JSON line (not a bench line)."""
-    import openfly_gb300 as fly
-    from openfly_gb300 import search as S
-    from openfly_gb300 import workloads as W
-    from openfly_gb300.build import build
-
-    build()
-    eam = fly.EAM(W.TABLE)
-    opt = S.DimerOptions.defaults(n=6, rot_n=6, f2norm=1e-3, max_steps=1000)
-    cl = W.search_clusters(n=args.searches, seed=7)
-    b = S.Batch(eam, [S.from_cluster(c) for c in cl], precision=fly.MIXED, dimer=opt)
-    b.set_stragglers(0)
-    b.run(S.Tuning(8, 256, 2, 128))
-    res, _, _ = b.results(positions=False)
-    tail = [k for k, r in enumerate(res) if r["steps"] > 100]
-    bt = S.Batch(eam, [S.from_cluster(cl[k]) for k in tail], precision=fly.MIXED, dimer=opt)
-    bt.set_stragglers(0)
-    t0 = time.perf_counter()
-    bt.run(S.Tuning(4, 256, 1, 0))
-    r2, _, _ = bt.results(positions=False)
-    print(json.dumps({"search_tail": len(tail), "seconds": time.perf_counter() - t0,
-                      "max_grad_calls": int(max(r["grad_calls"] for r in r2))}), flush=True)
-
-
-def prefactor_only(args) -> None:
-    """Only the prefactor step (hessian_prefactor: one 610-atom cluster, then a batch of 32), for
-    profiling the Hessian kernels; prints one JSON line (not a bench line)."""
-    import openfly_gb300 as fly
-    from openfly_gb300 import workloads as W
-    from openfly_gb300.build import build
-
-    build()
-    print(json.dumps({"prefactor": hessian_prefactor(fly, fly.EAM(W.TABLE))}), flush=True)
-
-
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--gpus", type=int, default=1)
@@ -769,26 +798,10 @@ def main():
     ap.add_argument("--plain-sample", type=int, default=32, help="searches timed on the plain path")
     ap.add_argument("--arrival-rate", type=float, default=3000.0, help="served requests per second (Poisson)")
     ap.add_argument("--steps-per-tick", type=int, default=8, help="translation steps per serving tick")
-    ap.add_argument("--search-batch", type=int, default=0,
-                    help="only run one batch of this many cluster searches (a small case for profilers)")
-    ap.add_argument("--max-search-steps", type=int, default=1000, help="translation-step limit of --search-batch")
-    ap.add_argument("--precision", choices=["mixed", "fp64"], default="mixed", help="precision of --search-batch")
-    ap.add_argument("--prefactor", action="store_true",
-                    help="only run the Hessian prefactor step (profiling the Hessian kernels)")
-    ap.add_argument("--search-tail", action="store_true",
-                    help="only run the searches of a cluster batch that outlast 100 steps, in one launch (profiling)")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")
-    if args.search_tail:
-        search_tail(args)
-        return
-    if args.prefactor:
-        prefactor_only(args)
-        return
-    if args.search_batch > 0:
-        search_batch(args)
-    elif args.impl == "reference":
+    if args.impl == "reference":
         reference_arm(args)
     else:
         ours(args)

@@ -142,9 +142,11 @@ int flygpu_hessian_eigenvalues(flygpu_eam* eam, flygpu_list* list, const uint32_
  * from device inputs into device outputs, and allocates nothing: its scratch is a fixed array inside
  * the library (about 33 KB per GPU, held until the process exits) and pairs are found by a minimum-image
  * scan without a neighbour list (periodic extents must exceed twice the cut-off). The first call on
- * each device looks up that array's device address, so make the first call before any stream capture.
- * Calls share the array, so calls that overlap on the GPU race; the call waits for its stream before
- * returning so it can report spline and type errors. Larger systems are rejected with
+ * each device looks up that array's device address (and may load the library's device code on that
+ * device), so make the first call before any stream capture. The address is kept for the life of the
+ * process: it does not survive cudaDeviceReset. Calls share the array, so calls that overlap on the GPU
+ * race. Every call copies the kernels' error word back to a host variable and waits for its stream to
+ * finish before returning, so it can report spline and type errors. Larger systems are rejected with
  * FLYGPU_INVALID_ARG. d_pos: 3n doubles; d_grad: 3n doubles; d_energy: 1 double. */
 #define FLYGPU_NOALLOC_MAX_ATOMS 4096
 int flygpu_eam_energy_gradient_noalloc(const flygpu_eam* eam, const double* d_pos, const uint32_t* d_types,

@@ -236,6 +236,11 @@ namespace flygpu {
     std::vector<int> cols;
     for (std::int64_t i = 0; i < n; ++i)
       if (!h_frozen[i]) cols.push_back(static_cast<int>(i));
+    // The column kernel skips frozen rows by the device flags: upload the same flags the active columns
+    // come from, so rows and columns always agree.
+    L->frozen.reserve(static_cast<std::size_t>(n) + 1);
+    FLY_CUDA(cudaMemcpyAsync(L->frozen.p, h_frozen, static_cast<std::size_t>(n), cudaMemcpyHostToDevice, s));
+    L->frozen_set = true;
     P.cols.reserve(std::max<std::size_t>(cols.size(), 1));
     if (!cols.empty())
       FLY_CUDA(cudaMemcpyAsync(P.cols.p, cols.data(), sizeof(int) * cols.size(), cudaMemcpyHostToDevice, s));

@@ -6,8 +6,8 @@ Reads the reference's test sources as text (it cannot be compiled here) and extr
   tests/potential/EAM/data.cpp  f_Fe(0), f_Fe(0.02) (lines 42-43)
   tests/neigh/adjacent.cpp      AdjacentCells of a 5^3 grid: interior order, face/edge/corner counts
   tests/system/boxes/hypergrid.cpp  HyperGrid(10, 3).cell_idx at 0, 5, 9.5
-Run from the repository root with the reference checked out at REFERENCE (default /root/reference):
-    python tests/golden/make_golden.py
+Run from the repository root with the REFERENCE environment variable naming the reference's checkout:
+    REFERENCE=<path to openFLY> python tests/golden/make_golden.py
 """
 from __future__ import annotations
 
@@ -17,7 +17,7 @@ import os
 import re
 import sys
 
-REF = os.environ.get("REFERENCE", "/root/reference")
+REF = os.environ.get("REFERENCE", "")
 OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_kats.json")
 
 
@@ -32,6 +32,8 @@ def arith(expr: str) -> int:
 
 
 def main() -> None:
+    if not REF or not os.path.isdir(REF):
+        sys.exit("set REFERENCE to the path of the reference's checkout")
     eam = open(os.path.join(REF, "tests/potential/EAM/eam.cpp")).read()
     data = open(os.path.join(REF, "tests/potential/EAM/data.cpp")).read()
     adj = open(os.path.join(REF, "tests/neigh/adjacent.cpp")).read()

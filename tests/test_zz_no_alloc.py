@@ -63,6 +63,36 @@ def test_noalloc_matches_allocating_entry_point(gpu, geam, noalloc):
         assert np.all(g[s.frozen == 1] == 0)
 
 
+def test_noalloc_allocates_nothing_and_clears_its_error_word(gpu, geam, noalloc):
+    # After a first call (which may load the library's device code), a call leaves the device's free
+    # memory unchanged. A call with a type index beyond the potential's types is rejected; the next valid
+    # call starts from a cleared error word and succeeds with the allocating entry point's results.
+    import torch
+
+    s = W.fe_vacancy_cell()
+    call(gpu, noalloc, geam, s)
+    dev = torch.device("cuda", 0)
+    pos = torch.tensor(s.pos.reshape(-1), dtype=torch.float64, device=dev)
+    bad_types = torch.full((s.n,), 7, dtype=torch.int32, device=dev)
+    frozen = torch.tensor(s.frozen, device=dev)
+    grad = torch.empty(3 * s.n, dtype=torch.float64, device=dev)
+    energy = torch.empty(1, dtype=torch.float64, device=dev)
+    ext = np.ascontiguousarray(s.extents, dtype=np.float64)
+    per = np.ascontiguousarray(s.periodic, dtype=np.int32)
+    stream = torch.cuda.current_stream(dev).cuda_stream
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info(dev)
+    st = noalloc(geam.h, pos.data_ptr(), bad_types.data_ptr(), frozen.data_ptr(), s.n, ext.ctypes.data,
+                 per.ctypes.data, energy.data_ptr(), grad.data_ptr(), stream)
+    free1, _ = torch.cuda.mem_get_info(dev)
+    assert st == gpu.INVALID_ARG
+    assert free1 == free0
+    e, g = call(gpu, noalloc, geam, s)
+    e_ref, g_ref = allocating(gpu, geam, s)
+    assert abs(e - e_ref) <= TOL * abs(e_ref)
+    assert np.linalg.norm(g - g_ref) <= TOL * np.linalg.norm(g_ref)
+
+
 def test_noalloc_rejects_oversized_systems(gpu, geam, noalloc):
     ext = np.full(3, 100.0)
     per = np.zeros(3, np.int32)
