@@ -319,8 +319,8 @@ int flygpu_minimise(flygpu_eam* eam, const flygpu_lbfgs_options* lbfgs, int prec
  * find.cpp:838-871): for each system EAM::hessian, Hessian::mass_weight and Hessian::eigenvalues as
  * flygpu_hessian_eigenvalues computes them, with each system's own list at the potential's cut-off.
  * systems: n, pos, types, frozen, extents and periodic of each descriptor are read (the search fields are
- * ignored). The systems run on `workers` host threads (<= 0: 8), each with its own stream, list and
- * solver handle, so their latency-bound eigensolves overlap on the GPU. eig: the 3 n_k ascending
+ * ignored). The systems run on `workers` host threads (<= 0: 8), each with its own stream and list, so
+ * their eigensolves (each one thread-block cluster of up to 16 SMs) overlap on the GPU. eig: the 3 n_k ascending
  * eigenvalues of every system, concatenated in order. masses: per type, NULL for the file's. */
 int flygpu_hessian_eigenvalues_batch(flygpu_eam* eam, const flygpu_search_desc* systems, int n_systems,
                                      const double* masses, int workers, double* eig);

@@ -61,7 +61,7 @@ def build(verbose: bool = False) -> str:
     with ThreadPoolExecutor(max_workers=max(1, min(len(srcs), os.cpu_count() or 8))) as ex:
         objs = list(ex.map(lambda s: _compile(nvcc, s, verbose), srcs))
     if not os.path.exists(LIB) or os.path.getmtime(LIB) < max(os.path.getmtime(o) for o in objs):
-        cmd = [nvcc, *ARCH, "-shared", "-o", LIB + ".tmp", *objs, "-lcudart", "-lcusolver"]
+        cmd = [nvcc, *ARCH, "-shared", "-o", LIB + ".tmp", *objs, "-lcudart"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

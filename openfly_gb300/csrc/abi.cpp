@@ -427,7 +427,7 @@ int flygpu_hessian_eigenvalues_batch(flygpu_eam* eam, const flygpu_search_desc* 
     int dev = 0;
     FLY_CUDA(cudaGetDevice(&dev));
     auto work = [&](int w) {
-      // worker w: systems w, w + P, ... on its own stream, list and solver handle; every CUDA call sits
+      // worker w: systems w, w + P, ... on its own stream and list (with its scratch); every CUDA call sits
       // inside guard (an exception must not leave the thread)
       std::unique_ptr<flygpu_list> L;
       for (int k = w; k < n_systems; k += P) {

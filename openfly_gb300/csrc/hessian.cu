@@ -17,11 +17,9 @@
 //
 // Hessian::mass_weight (system/hessian.hpp:136-143) scales block (j, i) by 1/sqrt(m_i m_j), and
 // Hessian::eigenvalues (system/hessian.hpp:86-93, Eigen's SelfAdjointEigenSolver on the lower
-// triangle) becomes cuSOLVER's symmetric eigensolver on the same triangle (the row-major lower triangle
-// is the column-major upper one), applied to the active atoms' block only: frozen atoms' rows and
-// columns are zero, so each frozen coordinate adds one exact zero eigenvalue.
-
-#include <cusolverDn.h>
+// triangle) becomes this library's dense symmetric eigensolver (eigen.cu) on the same triangle, applied
+// to the active atoms' block only: frozen atoms' rows and columns are zero, so each frozen coordinate
+// adds one exact zero eigenvalue.
 
 #include <memory>
 
@@ -216,15 +214,6 @@ namespace flygpu {
       H[e] *= 1 / sqrt(m3[col] * m3[row]);
     }
 
-    // Rows and columns of the active coordinates: out (M x M) = H[act[r], act[c]].
-    __global__ void k_gather_active(double const* __restrict__ H, std::int64_t N, int const* __restrict__ act,
-                                    std::int64_t M, double* __restrict__ out) {
-      std::int64_t const e = static_cast<std::int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-      if (e >= M * M) return;
-      std::int64_t const r = e / M, c = e - r * M;
-      out[e] = H[static_cast<std::int64_t>(act[r]) * N + act[c]];
-    }
-
   }  // namespace
 
   // Dense 3n x 3n Hessian into d_H (device, row-major). Synchronises the list's stream.
@@ -283,45 +272,6 @@ namespace flygpu {
     FLY_CUDA(cudaStreamSynchronize(s));
   }
 
-  namespace {
-    void solver_check(cusolverStatus_t st, char const* what) {
-      if (st == CUSOLVER_STATUS_ALLOC_FAILED) fail(FLYGPU_OOM, what);
-      if (st != CUSOLVER_STATUS_SUCCESS) fail(FLYGPU_CUDA_ERROR, std::string(what) + " failed (cuSOLVER status " + std::to_string(static_cast<int>(st)) + ")");
-    }
-  }  // namespace
-
-  // Eigenvalues (ascending) of the symmetric matrix whose row-major lower triangle d_H holds; d_H is
-  // overwritten. h_eig: N doubles on the host.
-  void symmetric_eigenvalues(flygpu_list* L, double* d_H, std::int64_t N, double* h_eig) {
-    if (N == 0) return;
-    if (N > 46340) fail(FLYGPU_INVALID_ARG, "Hessian too large for the dense eigensolver");
-    cudaStream_t const s = L->stream;
-    if (!L->solver) {
-      cusolverDnHandle_t h = nullptr;
-      solver_check(cusolverDnCreate(&h), "cusolverDnCreate");
-      L->solver = std::shared_ptr<void>(h, [](void* p) { cusolverDnDestroy(static_cast<cusolverDnHandle_t>(p)); });
-    }
-    auto const h = static_cast<cusolverDnHandle_t>(L->solver.get());
-    solver_check(cusolverDnSetStream(h, s), "cusolverDnSetStream");
-    int const n = static_cast<int>(N);
-    int lwork = 0;
-    solver_check(cusolverDnDsyevd_bufferSize(h, CUSOLVER_EIG_MODE_NOVECTOR, CUBLAS_FILL_MODE_UPPER, n, d_H, n, d_H, &lwork),
-                 "cusolverDnDsyevd_bufferSize");
-    // workspace, then N eigenvalues, then the info word (as a double slot)
-    std::size_t const lw = static_cast<std::size_t>(std::max(lwork, 1));
-    L->solver_work.reserve(lw + static_cast<std::size_t>(N) + 1);
-    double* const work = L->solver_work.p;
-    double* const w = work + lw;
-    int* const info = reinterpret_cast<int*>(w + N);
-    solver_check(cusolverDnDsyevd(h, CUSOLVER_EIG_MODE_NOVECTOR, CUBLAS_FILL_MODE_UPPER, n, d_H, n, w, work, lwork, info),
-                 "cusolverDnDsyevd");
-    int h_info = 0;
-    FLY_CUDA(cudaMemcpyAsync(&h_info, info, sizeof(int), cudaMemcpyDeviceToHost, s));
-    FLY_CUDA(cudaMemcpyAsync(h_eig, w, sizeof(double) * static_cast<std::size_t>(N), cudaMemcpyDeviceToHost, s));
-    FLY_CUDA(cudaStreamSynchronize(s));
-    if (h_info != 0) fail(FLYGPU_CUDA_ERROR, "symmetric eigensolver did not converge (info " + std::to_string(h_info) + ")");
-  }
-
   // Eigenvalues of a Hessian whose frozen atoms' rows and columns are zero: the matrix is block diagonal
   // (after a permutation) with the active coordinates' block and a zero block, so its spectrum is the
   // active block's eigenvalues and one exact zero per frozen coordinate. Only the active block is
@@ -329,26 +279,17 @@ namespace flygpu {
   // left unchanged when some atoms are frozen.
   void hessian_eigenvalues(flygpu_list* L, double* d_H, std::uint8_t const* h_frozen, double* h_eig) {
     std::int64_t const n = L->n, N = 3 * n;
-    cudaStream_t const s = L->stream;
     std::vector<int> act;
     for (std::int64_t i = 0; i < n; ++i)
       if (!h_frozen[i])
         for (int k = 0; k < 3; ++k) act.push_back(static_cast<int>(3 * i + k));
     std::int64_t const M = static_cast<std::int64_t>(act.size());
     if (M == N) {
-      symmetric_eigenvalues(L, d_H, N, h_eig);
+      dense_eigenvalues(L, d_H, N, {}, h_eig);
       return;
     }
     std::vector<double> w(static_cast<std::size_t>(M));
-    if (M > 0) {
-      DevBuf<int>& d_act = L->hs.act;
-      DevBuf<double>& sub = L->hs.sub;
-      d_act.reserve(static_cast<std::size_t>(M));
-      sub.reserve(static_cast<std::size_t>(M * M));
-      FLY_CUDA(cudaMemcpyAsync(d_act.p, act.data(), sizeof(int) * act.size(), cudaMemcpyHostToDevice, s));
-      launch(k_gather_active, static_cast<unsigned>((M * M + 255) / 256), 256, 0, s, d_H, N, d_act.p, M, sub.p);
-      symmetric_eigenvalues(L, sub.p, M, w.data());
-    }
+    if (M > 0) dense_eigenvalues(L, d_H, N, act, w.data());
     std::size_t const zeros = static_cast<std::size_t>(N - M);
     std::size_t j = 0, o = 0;
     while (j < w.size() && w[j] < 0) h_eig[o++] = w[j++];

@@ -205,8 +205,11 @@ namespace flygpu {
   struct HessianScratch {
     DevBuf<long long> offs;
     DevBuf<int> idx, act, cols;
-    DevBuf<double> dr, rho_mu, fder, m3, sub, H;
+    DevBuf<double> dr, rho_mu, fder, m3, sub, H, tri;
   };
+
+  // Largest matrix the dense eigensolver takes (three vectors of this many doubles in shared memory).
+  constexpr int MAX_DENSE_EIG = 9000;
 
 }  // namespace flygpu
 
@@ -252,8 +255,6 @@ struct flygpu_list {
   bool packed_valid = false;
   // CUDA-event timing of the main kernels (enabled by flygpu_list_set_timing)
   bool timing = false;
-  std::shared_ptr<void> solver;  // cuSOLVER handle of the Hessian eigensolves (created on first use)
-  flygpu::DevBuf<double> solver_work;
   flygpu::HessianScratch hs;
   flygpu::DevBuf<int> export_counts;  // per-atom counts of list_export_device
   std::vector<cudaEvent_t> ev_pool;
@@ -308,8 +309,9 @@ namespace flygpu {
   void eam_hessian(flygpu_eam const* E, flygpu_list* L, std::uint8_t const* h_frozen, double* d_H);
   void hessian_mass_weight(flygpu_eam const* E, flygpu_list* L, double const* type_mass, std::uint32_t const* h_types,
                            double* d_H);
-  // The solver handle and workspace are the list's (L->solver, L->solver_work), on the list's stream.
-  void symmetric_eigenvalues(flygpu_list* L, double* d_H, std::int64_t N, double* h_eig);
+  // eigen.cu: ascending eigenvalues of the symmetric matrix given by the row-major lower triangle of the
+  // N x N d_H, restricted to the coordinates `act` (all of them when act is empty); d_H is not modified.
+  void dense_eigenvalues(flygpu_list* L, double const* d_H, std::int64_t N, std::vector<int> const& act, double* h_eig);
   // The same for a 3n x 3n Hessian whose frozen atoms' rows and columns are zero (only the active block
   // is diagonalised; one exact zero per frozen coordinate is merged in).
   void hessian_eigenvalues(flygpu_list* L, double* d_H, std::uint8_t const* h_frozen, double* h_eig);
