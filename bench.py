@@ -348,10 +348,11 @@ def search_metrics(fly, args) -> dict:
     out["batched"]["batched_over_plain"] = out["batched"]["mixed"]["searches_per_s"] / plain
     # served stream: Poisson arrivals at --arrival-rate, then every request at once (capacity)
     stream = [S.from_cluster(c) for _, c in W.served_requests()]
-    # served with the batch's lanes and threads at one CTA per SM and the compiler's register allocation:
-    # the lowest latency per search (a served request waits on its own chain, not on the batch's tail)
+    # served in a latency shape: the batch's lanes per atom, 512 threads at one CTA per SM with the
+    # 128-register variant (a served request waits on its own chain, not on the batch's tail; at this
+    # arrival rate a few dozen requests are in flight, so SMs are not the scarce resource)
     t3 = out["batched"]["mixed"]["tuning"]
-    tune = S.Tuning(t3["lanes_per_atom"], t3["threads"], 1, 0)
+    tune = S.Tuning(t3["lanes_per_atom"], 512, 1, 128)
     out["served"] = serve_run(S, eam, stream, tune, opt, args, args.arrival_rate)
     out["served"]["tuning"] = tune.as_dict()
     out["served"]["plain_service_p50_ms"] = out["batched"]["plain_one_at_a_time"]["p50_ms"]
@@ -797,7 +798,7 @@ def main():
     ap.add_argument("--searches", type=int, default=4096, help="clusters in the batched search run")
     ap.add_argument("--plain-sample", type=int, default=32, help="searches timed on the plain path")
     ap.add_argument("--arrival-rate", type=float, default=3000.0, help="served requests per second (Poisson)")
-    ap.add_argument("--steps-per-tick", type=int, default=8, help="translation steps per serving tick")
+    ap.add_argument("--steps-per-tick", type=int, default=4, help="translation steps per serving tick")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")

@@ -92,6 +92,7 @@ struct flygpu_server {
   ~flygpu_server();
   void loop();
   void tick_graph();
+  void tick_body();  // the tick's work, recorded by tick_graph
   void admit(std::unique_lock<std::mutex>& lk);
   void retire();
 };
@@ -119,9 +120,27 @@ namespace {
 
 // One tick as a graph: upload the active list, reset the work counter, run the searches for
 // steps_per_tick steps, read every slot's state back. Inactive slots are marked done on the device.
+// A failure inside the capture ends it (and drops the partial graph) before the error propagates, so
+// the calling thread is never left inside an open capture.
 void flygpu_server::tick_graph() {
-  cudaGraph_t g;
   FLY_CUDA(cudaStreamBeginCapture(compute, cudaStreamCaptureModeThreadLocal));
+  try {
+    tick_body();
+  } catch (...) {
+    cudaGraph_t dead = nullptr;
+    cudaStreamEndCapture(compute, &dead);
+    if (dead) cudaGraphDestroy(dead);
+    cudaGetLastError();
+    throw;
+  }
+  cudaGraph_t g = nullptr;
+  FLY_CUDA(cudaStreamEndCapture(compute, &g));
+  cudaError_t const e = cudaGraphInstantiate(&graph, g, 0);
+  cudaGraphDestroy(g);
+  FLY_CUDA(e);
+}
+
+void flygpu_server::tick_body() {
   FLY_CUDA(cudaMemcpyAsync(order.p, h_order.p, sizeof(int) * static_cast<std::size_t>(max_active + 1),
                            cudaMemcpyHostToDevice, compute));
   FLY_CUDA(cudaMemsetAsync(work.p, 0, sizeof(int), compute));
@@ -146,9 +165,6 @@ void flygpu_server::tick_graph() {
   search_launch(v, tuning.lanes_per_atom, tuning.threads, tuning.max_registers, blocks, mixed, compute);
   FLY_CUDA(cudaMemcpyAsync(h_S.p, S.p, sizeof(SearchDev) * static_cast<std::size_t>(max_active), cudaMemcpyDeviceToHost,
                            compute));
-  FLY_CUDA(cudaStreamEndCapture(compute, &g));
-  FLY_CUDA(cudaGraphInstantiate(&graph, g, 0));
-  cudaGraphDestroy(g);
 }
 
 flygpu_server::~flygpu_server() {
@@ -313,6 +329,18 @@ int flygpu_server_create(flygpu_eam* eam, const flygpu_dimer_options* dimer, con
     srv->steps_per_tick = steps_per_tick;
     srv->budget = hbm_budget_bytes;
     if (tuning) srv->tuning = *tuning;
+    {  // the launch shape must fit one SM with the server's staging budget (checked before any capture)
+      flygpu_tuning const& t = srv->tuning;
+      if (t.lanes_per_atom != 1 && t.lanes_per_atom != 2 && t.lanes_per_atom != 4 && t.lanes_per_atom != 8)
+        fail(FLYGPU_INVALID_ARG, "lanes_per_atom must be 1, 2, 4 or 8");
+      if (t.threads % 32 != 0 || t.threads < 64 || t.threads > 1024)
+        fail(FLYGPU_INVALID_ARG, "threads must be 64..1024, a multiple of 32");
+      int bps = 0;
+      search_occupancy(t.lanes_per_atom, t.threads, srv->mixed, t.max_registers, SEARCH_SMEM_CAP, &bps);
+      if (bps < 1)
+        fail(FLYGPU_INVALID_ARG, "the server's launch shape does not fit an SM (threads x registers a thread, or shared "
+                                 "memory): use fewer threads or max_registers = 128");
+    }
     {  // keep freed request blocks in the pool instead of returning them to the driver
       int dev = 0;
       cudaMemPool_t pool;

@@ -110,3 +110,16 @@ def test_submit_many_is_all_or_nothing(gpu, geam, S, requests):
     for i, x in zip(ids, single):
         assert got[i][0]["energy"] == x[0]["energy"]
         assert np.array_equal(got[i][1], x[1])
+
+
+def test_server_rejects_a_shape_that_cannot_launch(gpu, geam, S, requests):
+    # 1024 threads with the compiler's register allocation do not fit an SM: rejected when the server is
+    # created, before its graph is captured; the thread is not left inside a capture, so a server with a
+    # valid shape works afterwards.
+    opt = S.DimerOptions.defaults(f2norm=1e-3, n=6)
+    with pytest.raises(gpu.FlyGPUError) as e:
+        S.Server(geam, precision=gpu.MIXED, tuning=S.Tuning(8, 1024, 1, 0), dimer=opt)
+    assert e.value.status == gpu.INVALID_ARG
+    served, stats = serve_all(S, gpu, geam, requests[:2], opt, S.Tuning(4, 128, 2))
+    assert stats["completed"] == 2
+    assert all(r[0]["status"] == 0 for r in served)
