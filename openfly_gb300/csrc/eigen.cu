@@ -17,10 +17,11 @@
 // d_k = A[k, k], e_k = alpha. Every CTA runs the same loop with the same trip count and no early exit, so
 // every barrier is reached by all of them (hardware cluster barriers, not spin loops). On the global path
 // the rows are read with ld.global.cg (L2, not L1) after the barriers' release/acquire.
-// GB300 issues binary64 at about 1/64 of the binary32 rate and a dependent binary64 operation takes ~67
-// cycles, so the kernel spends binary64 instructions only where they carry the algorithm: reductions
-// run on the warps that hold data, the update is two fused multiply-adds an element, and rows are
-// walked in full groups of four plus a one-wide tail (no masked lanes).
+// GB300 issues binary64 at about 1/64 of the binary32 rate (1.6 lanes a clock per SM) and a dependent
+// binary64 operation takes ~67 cycles, so the O(M^3) work (the rows, u, w, p and every dot product) is
+// float-float arithmetic on the binary32 units (~48 significant bits, far inside the eigenvalues'
+// 1e-10-of-the-spectral-radius tolerance), and so are the per-step scalars. Reductions run on the
+// warps that hold data, and rows are walked in full groups of four plus a one-wide tail.
 // Stage 2, k_bisect: the tridiagonal's eigenvalues by Sturm-sequence multisection, one warp per
 // eigenvalue index j: the 32 lanes count the eigenvalues below 32 points of the current interval (sign
 // changes of the leading principal minors of T - x I, a division-free three-term recurrence), the
@@ -45,75 +46,97 @@ namespace flygpu {
     constexpr int TW = TT / 32;
     constexpr int TRIDIAG_SMEM_MAX = 220 * 1024;  // dynamic shared memory limit set on k_tridiag
 
-    // sqrt(a) and 1 / a from binary32 seeds and Newton steps in binary64 (each a short chain of FMAs;
-    // the correctly rounded library forms are long dependent chains at 67 cycles a binary64 operation).
-    // Accurate to a few ulp for a in the binary32 exponent range, which the caller checks.
-    __device__ inline double fast_rsqrt(double a) {
-      double y = static_cast<double>(rsqrtf(static_cast<float>(a)));
-      double const h = 0.5 * a;
-      y = y * fma(-h * y, y, 1.5);
-      y = y * fma(-h * y, y, 1.5);
-      return y * fma(-h * y, y, 1.5);
+    // ------------------------------------------------------------------ float-float arithmetic
+    // A value as an unevaluated sum hi + lo of two binary32 numbers (|lo| <= ulp(hi) / 2): about 48
+    // significant bits, from binary32 instructions only. The error-free steps (TwoSum, the FMA split of a
+    // product) use the _rn intrinsics so the compiler cannot fuse or reorder them.
+    struct ff {
+      float hi, lo;
+    };
+    __device__ inline ff ff_of(double d) {
+      float const h = __double2float_rn(d);
+      return {h, __double2float_rn(d - static_cast<double>(h))};
     }
-    __device__ inline double fast_rcp(double a) {
-      double y = static_cast<double>(__frcp_rn(static_cast<float>(a)));
-      y = y * fma(-a, y, 2.0);
-      y = y * fma(-a, y, 2.0);
-      return y * fma(-a, y, 2.0);
+    __device__ inline double ff_dbl(ff a) { return static_cast<double>(a.hi) + static_cast<double>(a.lo); }
+    __device__ inline ff quick_two_sum(float a, float b) {  // |a| >= |b| or a == 0
+      float const s = __fadd_rn(a, b);
+      return {s, __fsub_rn(b, __fsub_rn(s, a))};
     }
-    __device__ inline bool f32_range(double a) { return a > 1e-30 && a < 1e30; }
+    __device__ inline ff ff_add(ff a, ff b) {
+      float const s = __fadd_rn(a.hi, b.hi);
+      float const bb = __fsub_rn(s, a.hi);
+      float const e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(b.hi, bb));
+      return quick_two_sum(s, __fadd_rn(e, __fadd_rn(a.lo, b.lo)));
+    }
+    __device__ inline ff ff_mul(ff a, ff b) {
+      float const p = __fmul_rn(a.hi, b.hi);
+      float e = fmaf(a.hi, b.hi, -p);
+      e = fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, e));
+      return quick_two_sum(p, e);
+    }
+    __device__ inline ff ff_neg(ff a) { return {-a.hi, -a.lo}; }
+    __device__ inline ff ff_shfl_down(ff a, int o) {
+      return {__shfl_down_sync(0xffffffffu, a.hi, o), __shfl_down_sync(0xffffffffu, a.lo, o)};
+    }
+    __device__ inline ff ff_shfl_xor(ff a, int o) {
+      return {__shfl_xor_sync(0xffffffffu, a.hi, o), __shfl_xor_sync(0xffffffffu, a.lo, o)};
+    }
 
     // Sum over the CTA of v, where only warps w < nw hold data: their lanes reduce with shuffles, their
-    // leaders' sums are added by warp 0 (binary64 adds are the scarce resource; idle warps add nothing).
-    __device__ double cta_sum(double v, double* red, int nw) {
+    // leaders' sums are added by warp 0.
+    __device__ ff cta_sum(ff v, ff* red, int nw) {
       int const lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
       if (warp < nw) {
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        for (int o = 16; o > 0; o >>= 1) v = ff_add(v, ff_shfl_down(v, o));
         if (lane == 0) red[warp] = v;
       }
       __syncthreads();
       if (warp == 0) {
-        double t = lane < nw ? red[lane] : 0.0;
-        for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+        ff t = lane < nw ? red[lane] : ff{0.f, 0.f};
+        for (int o = 16; o > 0; o >>= 1) t = ff_add(t, ff_shfl_down(t, o));
         if (lane == 0) red[TW] = t;
       }
       __syncthreads();
-      double const s = red[TW];
+      ff const s = red[TW];
       __syncthreads();
       return s;
     }
 
-    // The rows of the matrix a CTA owns: in its shared memory (SM) or in the global matrix.
+    // The rows of the matrix a CTA owns: in its shared memory (SM) or in the global matrix, as float-float.
     template <bool SM>
     struct Rows {
-      double* base;  // SM: the CTA's rows, local row r at base + r M; else the global matrix
+      ff* base;  // SM: the CTA's rows, local row r at base + r M; else the global matrix
       int M, C;
-      __device__ double* own(int i) const {
+      __device__ ff* own(int i) const {
         return SM ? base + static_cast<std::int64_t>(i / C) * M : base + static_cast<std::int64_t>(i) * M;
       }
     };
 
     template <bool SM>
-    __device__ inline double ld(double const* p) {
+    __device__ inline ff ld(ff const* p) {
       if constexpr (SM) {
         return *p;
       } else {
-        return __ldcg(p);
+        float2 const v = __ldcg(reinterpret_cast<float2 const*>(p));
+        return {v.x, v.y};
       }
     }
     template <bool SM>
-    __device__ inline void st(double* p, double v) {
+    __device__ inline void st(ff* p, ff v) {
       if constexpr (SM) {
         *p = v;
       } else {
-        __stcg(p, v);
+        __stcg(reinterpret_cast<float2*>(p), make_float2(v.hi, v.lo));
       }
     }
 
-    // Householder tridiagonalisation of the M x M symmetric A (full storage; overwritten on the global
-    // path). d: M, e: M (e[M-1] unused). Launched as one cluster of C CTAs; CTA c owns the rows i with
-    // i mod C == c. With SM every CTA keeps its rows in shared memory (ceil(M / C) rows). Row k, the p
-    // values and the CTAs' shares of u^T p are read across the cluster through distributed shared memory.
+    // Householder tridiagonalisation of the M x M symmetric A (binary64, full storage; overwritten on
+    // the global path, where it is first converted in place to float-float). d: M, e: M (e[M-1]
+    // unused). Launched as one cluster of C CTAs; CTA c owns the rows i with i mod C == c. With SM every
+    // CTA keeps its rows in shared memory (ceil(M / C) rows). Row k, the p values and the CTAs' shares
+    // of u^T p are read across the cluster through distributed shared memory. The matrix, u, w, p and
+    // every dot product are float-float, and so are the per-step scalars |x|, alpha and tau (binary32
+    // seeds refined by one float-float Newton step).
     template <bool SM>
     __global__ void __launch_bounds__(TT) k_tridiag(double* __restrict__ A, int M, double* __restrict__ d,
                                                    double* __restrict__ e) {
@@ -121,111 +144,131 @@ namespace flygpu {
       int const C = static_cast<int>(cl.num_blocks());
       int const c = static_cast<int>(cl.block_rank());
       int const R = (M + C - 1) / C;
-      extern __shared__ double sm[];
-      double* rows = sm;                                              // SM: R x M
-      double* u = sm + (SM ? static_cast<std::int64_t>(R) * M : 0);  // M
-      double* w = u + M;                                              // M
-      double* pl = w + M;                                             // M: p_i of the owned rows, at index i
-      double* share = pl + M;                                         // 1
-      double* red = share + 1;                                        // TW + 1
+      extern __shared__ ff sm[];
+      ff* rows = sm;                                              // SM: R x M
+      ff* u = sm + (SM ? static_cast<std::int64_t>(R) * M : 0);  // M
+      ff* w = u + M;                                              // M
+      ff* pl = w + M;                                             // M: p_i of the owned rows, at index i
+      ff* share = pl + M;                                         // 1
+      ff* red = share + 1;                                        // TW + 1
       int const lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-      Rows<SM> const own{SM ? rows : A, M, C};
-      if (SM) {
-        for (int r = warp; r * C + c < M; r += TW)
-          for (int j = lane; j < M; j += 32)
-            rows[static_cast<std::int64_t>(r) * M + j] = __ldcg(A + static_cast<std::int64_t>(r * C + c) * M + j);
-        cl.sync();
-      }
+      ff* const Aff = reinterpret_cast<ff*>(A);  // the global path's rows, converted in place
+      Rows<SM> const own{SM ? rows : Aff, M, C};
+      for (int r = warp; r * C + c < M; r += TW)
+        for (int j = lane; j < M; j += 32) {
+          std::int64_t const g = static_cast<std::int64_t>(r * C + c) * M + j;
+          ff const v = ff_of(__ldcg(A + g));
+          if (SM) {
+            rows[static_cast<std::int64_t>(r) * M + j] = v;
+          } else {
+            st<false>(Aff + g, v);
+          }
+        }
+      cl.sync();
       for (int k = 0; k + 2 < M; ++k) {
         int const b = k + 1, m = M - b;
-        double const* rk = SM ? cl.map_shared_rank(rows, k % C) + static_cast<std::int64_t>(k / C) * M
-                              : A + static_cast<std::int64_t>(k) * M;
-        double s2 = 0;
+        ff const* rk = SM ? cl.map_shared_rank(rows, k % C) + static_cast<std::int64_t>(k / C) * M
+                          : Aff + static_cast<std::int64_t>(k) * M;
+        ff s2 = {0.f, 0.f};
         for (int j = threadIdx.x; j < m; j += TT) {
-          double const x = ld<SM>(rk + b + j);
+          ff const x = ld<SM>(rk + b + j);
           u[j] = x;
-          s2 = fma(x, x, s2);
+          s2 = ff_add(s2, ff_mul(x, x));
         }
         s2 = cta_sum(s2, red, min(TW, (m + 31) / 32));
-        double const x0 = u[0];
-        double const nrm = f32_range(s2) ? s2 * fast_rsqrt(s2) : sqrt(s2);
-        double const alpha = x0 > 0 ? -nrm : nrm;
-        double const den = alpha * alpha - alpha * x0;
+        // |x| and tau = 1 / (alpha^2 - alpha x0) from binary32 seeds with one float-float Newton step
+        ff const x0 = u[0];
+        float const sq = sqrtf(s2.hi);
+        ff nrm = {0.f, 0.f};
+        if (sq > 0.f) {
+          ff const r = ff_add(s2, ff_neg(ff_mul(ff{sq, 0.f}, ff{sq, 0.f})));
+          nrm = quick_two_sum(sq, __fdiv_rn(r.hi, 2.f * sq));
+        }
+        ff const alpha = x0.hi > 0.f ? ff_neg(nrm) : nrm;
+        ff const den = ff_add(ff_mul(alpha, alpha), ff_neg(ff_mul(alpha, x0)));
         // a column that is already zero below the sub-diagonal needs no reflection (tau = 0)
-        double const tau = den > 0 && s2 - x0 * x0 > 0 ? (f32_range(den) ? fast_rcp(den) : 1.0 / den) : 0.0;
+        bool const reflect = den.hi > 0.f && ff_add(s2, ff_neg(ff_mul(x0, x0))).hi > 0.f;
+        ff tau = {0.f, 0.f};
+        if (reflect) {
+          float const r0 = __frcp_rn(den.hi);
+          ff const e1 = ff_add(ff{1.f, 0.f}, ff_neg(ff_mul(den, ff{r0, 0.f})));
+          tau = quick_two_sum(r0, __fmul_rn(r0, e1.hi));
+        }
         __syncthreads();
-        if (threadIdx.x == 0) u[0] = tau != 0.0 ? x0 - alpha : 0.0;
+        if (threadIdx.x == 0) u[0] = reflect ? ff_add(x0, ff_neg(alpha)) : ff{0.f, 0.f};
         if (c == 0 && threadIdx.x == 0) {
-          d[k] = ld<SM>(rk + k);
-          e[k] = tau != 0.0 ? alpha : x0;
+          d[k] = ff_dbl(ld<SM>(rk + k));
+          e[k] = ff_dbl(reflect ? alpha : x0);
         }
         __syncthreads();
         // p_i = tau (A u)_i over owned rows, and the share of u^T p. Each lane keeps four independent
-        // partial sums (loads in groups of 4), so a row's dependent chain is a quarter of its length.
-        double sh = 0;
+        // partial sums, so a row's dependent chain is a quarter of its length.
+        ff sh = {0.f, 0.f};
         for (int r = warp; r * C + c < M; r += TW) {
           int const i = r * C + c;
           if (i < b) continue;
-          double const* ri = own.own(i) + b;
-          double acc[4] = {0, 0, 0, 0};
+          ff const* ri = own.own(i) + b;
+          ff acc[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
           int j = lane;
           for (; j + 96 < m; j += 128) {
-            double v[4];
+            ff v[4];
 #pragma unroll
             for (int t = 0; t < 4; ++t) v[t] = ld<SM>(ri + j + 32 * t);
 #pragma unroll
-            for (int t = 0; t < 4; ++t) acc[t] = fma(v[t], u[j + 32 * t], acc[t]);
+            for (int t = 0; t < 4; ++t) acc[t] = ff_add(acc[t], ff_mul(v[t], u[j + 32 * t]));
           }
-          for (; j < m; j += 32) acc[0] = fma(ld<SM>(ri + j), u[j], acc[0]);
-          double a = (acc[0] + acc[1]) + (acc[2] + acc[3]);
-          for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+          for (; j < m; j += 32) acc[0] = ff_add(acc[0], ff_mul(ld<SM>(ri + j), u[j]));
+          ff a = ff_add(ff_add(acc[0], acc[1]), ff_add(acc[2], acc[3]));
+          for (int o = 16; o > 0; o >>= 1) a = ff_add(a, ff_shfl_down(a, o));
           if (lane == 0) {
-            double const pi = tau * a;
+            ff const pi = ff_mul(tau, a);
             pl[i] = pi;
-            sh = fma(u[i - b], pi, sh);
+            sh = ff_add(sh, ff_mul(u[i - b], pi));
           }
         }
         // the share: one value per warp leader, summed by warp 0
         if (lane == 0) red[warp] = sh;
         __syncthreads();
         if (warp == 0) {
-          double t = lane < TW ? red[lane] : 0.0;
-          for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+          ff t = lane < TW ? red[lane] : ff{0.f, 0.f};
+          for (int o = 16; o > 0; o >>= 1) t = ff_add(t, ff_shfl_down(t, o));
           if (lane == 0) *share = t;
         }
         cl.sync();
         // K = tau / 2 sum of the CTAs' shares: a shuffle tree in warp 0, broadcast through shared memory
         if (warp == 0) {
-          double t = lane < C ? *cl.map_shared_rank(share, lane) : 0.0;
-          for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-          if (lane == 0) red[TW] = 0.5 * tau * t;
+          ff t = lane < C ? *cl.map_shared_rank(share, lane) : ff{0.f, 0.f};
+          for (int o = 16; o > 0; o >>= 1) t = ff_add(t, ff_shfl_xor(t, o));
+          if (lane == 0) red[TW] = ff_mul(ff_mul(tau, t), ff{0.5f, 0.f});
         }
         __syncthreads();
-        double const K = red[TW];
-        for (int j = threadIdx.x; j < m; j += TT) w[j] = fma(-K, u[j], cl.map_shared_rank(pl, (b + j) % C)[b + j]);
+        ff const K = red[TW];
+        for (int j = threadIdx.x; j < m; j += TT)
+          w[j] = ff_add(cl.map_shared_rank(pl, (b + j) % C)[b + j], ff_neg(ff_mul(K, u[j])));
         __syncthreads();
         for (int r = warp; r * C + c < M; r += TW) {
           int const i = r * C + c;
           if (i < b) continue;
-          double* ri = own.own(i) + b;
-          double const ui = u[i - b], wi = w[i - b];
-          // A_ij - u_i w_j - w_i u_j as two fused multiply-adds
+          ff* ri = own.own(i) + b;
+          ff const ui = u[i - b], wi = w[i - b];
+          // A_ij - (u_i w_j + w_i u_j)
           int j = lane;
           for (; j + 96 < m; j += 128) {
-            double v[4];
+            ff v[4];
 #pragma unroll
             for (int t = 0; t < 4; ++t) v[t] = ld<SM>(ri + j + 32 * t);
 #pragma unroll
-            for (int t = 0; t < 4; ++t) st<SM>(ri + j + 32 * t, fma(-ui, w[j + 32 * t], fma(-wi, u[j + 32 * t], v[t])));
+            for (int t = 0; t < 4; ++t)
+              st<SM>(ri + j + 32 * t, ff_add(v[t], ff_neg(ff_add(ff_mul(ui, w[j + 32 * t]), ff_mul(wi, u[j + 32 * t])))));
           }
-          for (; j < m; j += 32) st<SM>(ri + j, fma(-ui, w[j], fma(-wi, u[j], ld<SM>(ri + j))));
+          for (; j < m; j += 32) st<SM>(ri + j, ff_add(ld<SM>(ri + j), ff_neg(ff_add(ff_mul(ui, w[j]), ff_mul(wi, u[j])))));
         }
         cl.sync();
       }
       if (c == 0 && threadIdx.x == 0) {
         auto at = [&](int i, int j) {
-          return SM ? cl.map_shared_rank(rows, i % C)[static_cast<std::int64_t>(i / C) * M + j]
-                    : __ldcg(A + static_cast<std::int64_t>(i) * M + j);
+          return ff_dbl(SM ? cl.map_shared_rank(rows, i % C)[static_cast<std::int64_t>(i / C) * M + j]
+                           : ld<false>(Aff + static_cast<std::int64_t>(i) * M + j));
         };
         if (M >= 2) {
           d[M - 2] = at(M - 2, M - 2);
@@ -310,7 +353,7 @@ namespace flygpu {
 
     std::size_t tridiag_smem(int M, int C, bool sm) {
       std::size_t const R = sm ? static_cast<std::size_t>((M + C - 1) / C) : 0;
-      return (R * static_cast<std::size_t>(M) + 3 * static_cast<std::size_t>(M) + 1 + TW + 1) * sizeof(double);
+      return (R * static_cast<std::size_t>(M) + 3 * static_cast<std::size_t>(M) + 1 + TW + 1) * sizeof(double);  // 8-byte elements
     }
 
     cudaLaunchConfig_t tridiag_config(int C, std::size_t smem, cudaLaunchAttribute& at, cudaStream_t s) {
