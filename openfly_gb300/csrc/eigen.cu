@@ -279,42 +279,38 @@ namespace flygpu {
       cl.sync();  // no CTA leaves while another may still read its shared memory
     }
 
-    // Number of eigenvalues of the tridiagonal (d, e2 = e^2) below x: the sign changes of the sequence
-    // 1, p_0, p_1, ... of leading principal minors of T - x I, p_i = (d_i - x) p_{i-1} - e_{i-1}^2 p_{i-2}
-    // (the Sturm sequence; no divisions, which cost dozens of binary64 instructions on this GPU). A zero
-    // minor takes the sign opposite to the one before it. Signs, zeros and magnitudes are read from the
-    // bit patterns with integer instructions; every 8 minors the last two are rescaled by a power of two
-    // when they leave [2^-600, 2^600] (8 steps cannot overflow from there), which keeps every sign.
-    __device__ inline bool neg(double v) { return __double_as_longlong(v) < 0; }
-    __device__ inline int expo(double v) { return static_cast<int>((__double_as_longlong(v) >> 52) & 0x7ff); }
-    __device__ inline bool is_zero(double v) { return (__double_as_longlong(v) << 1) == 0; }
-
-    __device__ int sturm_count(double const* __restrict__ d, double const* __restrict__ e2, int M, double x) {
-      double pm = 1.0, p = d[0] - x;
-      if (is_zero(p)) p = -0x1p-200;
-      int cnt = neg(p);
+    // Number of eigenvalues of the tridiagonal (d, e2 = e^2, as float-float) below x: the sign changes
+    // of the sequence 1, p_0, p_1, ... of leading principal minors of T - x I,
+    // p_i = (d_i - x) p_{i-1} - e_{i-1}^2 p_{i-2} (the Sturm sequence), in float-float arithmetic on the
+    // binary32 units and without divisions. A zero minor takes the sign opposite to the one before it.
+    // After every step the last two minors are rescaled by 2^-64 (2^64) when they leave [2^-60, 2^60]:
+    // power-of-two scaling is exact and keeps every sign, and binary32's exponent range is small.
+    __device__ int sturm_count(ff const* __restrict__ d, ff const* __restrict__ e2, int M, ff x) {
+      ff const nx = ff_neg(x);
+      ff pm = {1.f, 0.f};
+      ff p = ff_add(d[0], nx);
+      if (p.hi == 0.f) p = {-0x1p-40f, 0.f};
+      int cnt = p.hi < 0.f;
       for (int i = 1; i < M; ++i) {
-        double pn = fma(d[i] - x, p, -(e2[i - 1] * pm));
-        if (is_zero(pn)) pn = -p * 0x1p-200;
-        cnt += neg(pn) != neg(p);
+        ff pn = ff_add(ff_mul(ff_add(d[i], nx), p), ff_neg(ff_mul(e2[i - 1], pm)));
+        if (pn.hi == 0.f) pn = {-p.hi * 0x1p-40f, 0.f};
+        cnt += (pn.hi < 0.f) != (p.hi < 0.f);
         pm = p;
         p = pn;
-        if ((i & 7) == 0) {
-          int const ep = expo(p);
-          if (ep > 1023 + 600) {
-            p *= 0x1p-600;
-            pm *= 0x1p-600;
-          } else if (ep < 1023 - 600 && expo(pm) < 1023 - 600) {
-            p *= 0x1p600;
-            pm *= 0x1p600;
-          }
+        float const ap = fabsf(p.hi);
+        if (ap > 0x1p60f) {
+          p = {p.hi * 0x1p-64f, p.lo * 0x1p-64f};
+          pm = {pm.hi * 0x1p-64f, pm.lo * 0x1p-64f};
+        } else if (ap < 0x1p-60f && fabsf(pm.hi) < 0x1p-60f) {
+          p = {p.hi * 0x1p64f, p.lo * 0x1p64f};
+          pm = {pm.hi * 0x1p64f, pm.lo * 0x1p64f};
         }
       }
       return cnt;
     }
 
-    // One warp per eigenvalue index; bounds = {lo, hi, tol}.
-    __global__ void k_bisect(double const* __restrict__ d, double const* __restrict__ e2, int M,
+    // One warp per eigenvalue index; bounds = {lo, hi, tol} (binary64).
+    __global__ void k_bisect(ff const* __restrict__ d, ff const* __restrict__ e2, int M,
                              double const* __restrict__ bounds, double* __restrict__ eig) {
       int const lane = threadIdx.x & 31;
       int const j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -325,7 +321,7 @@ namespace flygpu {
         double const width = hi - lo;
         if (width <= fmax(tol, 4 * DBL_EPSILON * fmax(fabs(lo), fabs(hi)))) break;
         double const x = lo + width * (static_cast<double>(lane + 1) * (1.0 / 33.0));
-        int const cnt = sturm_count(d, e2, M, x);
+        int const cnt = sturm_count(d, e2, M, ff_of(x));
         unsigned const above = __ballot_sync(0xffffffffu, cnt > j);
         double const xs = __shfl_sync(0xffffffffu, x, above ? __ffs(above) - 1 : 31);
         if (above == 0u) {
@@ -417,7 +413,7 @@ namespace flygpu {
     cudaStream_t const s = L->stream;
     HessianScratch& P = L->hs;
     P.sub.reserve(static_cast<std::size_t>(M * M));
-    P.tri.reserve(4 * static_cast<std::size_t>(M) + 8);
+    P.tri.reserve(5 * static_cast<std::size_t>(M) + 8);
     int const* d_act = nullptr;
     if (!act.empty()) {
       P.act.reserve(act.size());
@@ -427,8 +423,8 @@ namespace flygpu {
     launch(k_sym_gather, static_cast<unsigned>((M * M + 255) / 256), 256, 0, s, d_H, N, d_act, M, P.sub.p);
     double* const dd = P.tri.p;
     double* const ee = dd + M;
-    double* const e2 = ee + M;
-    double* const ww = e2 + M;
+    double* const fb = ee + M;   // 2 M: d and e^2 as float-float (4 M floats)
+    double* const ww = fb + 2 * M;
     double* const bnd = ww + M;  // 3
     int const Mi = static_cast<int>(M);
     tridiag_launch(P.sub.p, Mi, dd, ee, s);
@@ -449,12 +445,24 @@ namespace flygpu {
       tnorm = std::max(tnorm, std::fabs(a) + el + er);
       if (i + 1 < M) he2[k] = he[k] * he[k];
     }
+    if (!(tnorm < 1e18)) fail(FLYGPU_INVALID_ARG, "matrix norm beyond the eigensolver's float-float range");
     double const pad = 2 * DBL_EPSILON * std::max(tnorm, DBL_MIN) * static_cast<double>(M) + DBL_MIN;
     double const hb[3] = {lo - pad, hi + pad, 2 * DBL_EPSILON * tnorm};
-    FLY_CUDA(cudaMemcpyAsync(e2, he2.data(), sizeof(double) * he2.size(), cudaMemcpyHostToDevice, s));
+    // d and e^2 as float-float pairs (hi, lo) for the multisection
+    std::vector<float> hff(4 * static_cast<std::size_t>(M));
+    for (std::int64_t i = 0; i < M; ++i) {
+      std::size_t const k = static_cast<std::size_t>(i);
+      float const dh = static_cast<float>(hd[k]), eh = static_cast<float>(he2[k]);
+      hff[2 * k] = dh;
+      hff[2 * k + 1] = static_cast<float>(hd[k] - static_cast<double>(dh));
+      hff[2 * static_cast<std::size_t>(M) + 2 * k] = eh;
+      hff[2 * static_cast<std::size_t>(M) + 2 * k + 1] = static_cast<float>(he2[k] - static_cast<double>(eh));
+    }
+    ff* const dff = reinterpret_cast<ff*>(fb);
+    FLY_CUDA(cudaMemcpyAsync(dff, hff.data(), sizeof(float) * hff.size(), cudaMemcpyHostToDevice, s));
     FLY_CUDA(cudaMemcpyAsync(bnd, hb, sizeof hb, cudaMemcpyHostToDevice, s));
-    // one warp per block: the warps spread over every SM (binary64 throughput is per SM)
-    launch(k_bisect, static_cast<unsigned>(M), 32, 0, s, static_cast<double const*>(dd), static_cast<double const*>(e2), Mi,
+    // one warp per block: the warps spread over every SM
+    launch(k_bisect, static_cast<unsigned>(M), 32, 0, s, static_cast<ff const*>(dff), static_cast<ff const*>(dff + M), Mi,
            static_cast<double const*>(bnd), ww);
     FLY_CUDA(cudaMemcpyAsync(h_eig, ww, sizeof(double) * static_cast<std::size_t>(M), cudaMemcpyDeviceToHost, s));
     FLY_CUDA(cudaStreamSynchronize(s));

@@ -243,7 +243,9 @@ namespace flygpu {
     std::size_t const N = 3 * static_cast<std::size_t>(n);
     FLY_CUDA(cudaMemsetAsync(d_H, 0, sizeof(double) * N * N, s));
     TablesView const tb = E->view();
-    launch(k_hess_rho, static_cast<unsigned>((n + 127) / 128), 128, 0, s, tb, n, P.offs.p, P.idx.p, P.dr.p, L->types.p,
+    // one warp per CTA: the per-atom binary64 work spreads over as many SMs as there are warps (binary64
+    // throughput is per SM), each thread's arithmetic unchanged
+    launch(k_hess_rho, static_cast<unsigned>((n + 31) / 32), 32, 0, s, tb, n, P.offs.p, P.idx.p, P.dr.p, L->types.p,
            P.rho_mu.p, P.fder.p, L->err.p);
     if (!cols.empty())
       launch(k_hess_col, static_cast<unsigned>(cols.size()), 32, 0, s, tb, n, P.cols.p, P.offs.p, P.idx.p, P.dr.p,
