@@ -54,7 +54,10 @@ def run_oracle(O, odata, opt, cl):
     return r
 
 
-def compare(results, refs, label, positions=None, min_same_exit=0.8, min_same_saddle=0.6):
+# Measured on the 32 test clusters: the same exit code for 100 % (binary64) and 97 % (binary32 pairs) of
+# searches, and every jointly converged pair on the same saddle; the bars leave room for one or two
+# chaotic searches more.
+def compare(results, refs, label, positions=None, min_same_exit=0.9, min_same_saddle=0.8):
     same_exit = sum(a["exit_code"] == b["exit"] for a, b in zip(results, refs))
     assert same_exit >= min_same_exit * len(refs), (label, [(a["exit_code"], b["exit"]) for a, b in zip(results, refs)])
     both = [k for k, (a, b) in enumerate(zip(results, refs)) if a["exit_code"] == 0 and b["exit"] == 0]
