@@ -3,8 +3,9 @@
 A dimer search can branch to a different saddle on rounding-level differences (reduction order,
 binary32 pair terms), as the reference's own results do across compilers and thread counts. So the
 bar is stated per saddle: when both runs converge to the same saddle (final positions within
-SAME_SADDLE_A of each other), their energies agree within 1 meV (the barrier-height bar); most
-searches end with the same exit code, and most jointly converged ones at the same saddle.
+SAME_SADDLE_A of each other), their energies agree within 1 meV (the barrier-height bar); at least
+90 % of searches end with the same exit code, and at least 80 % of jointly converged ones at the same
+saddle.
 """
 import numpy as np
 import pytest
