@@ -204,8 +204,9 @@ namespace flygpu {
   // cudaFree would synchronise the whole device and serialise concurrent callers).
   struct HessianScratch {
     DevBuf<long long> offs;
-    DevBuf<int> idx, act, cols;
-    DevBuf<double> dr, rho_mu, fder, m3, sub, H, tri;
+    DevBuf<int> idx, act, cols, key;
+    DevBuf<double> dr, rho_mu, fder, pr, pfp, m3, sub, H, tri;
+    DevBuf<std::uint32_t> ty;
   };
 
   // Largest matrix the dense eigensolver takes (three vectors of this many doubles in shared memory).

@@ -132,21 +132,27 @@ namespace flygpu {
     launch(k_gather_out, v.n_search, 128, 0, s, v, d_act3_off, out_x, out_ax);
   }
 
+  // The search kernels' shared-memory limit is a property of the current context (a device reset drops
+  // it), so it is set again before every occupancy query and every launch outside a stream capture, always
+  // to the same constant (concurrent host threads agree); a capture relies on search_init_kernels() having
+  // run just before it.
+  namespace {
+    void set_smem_cap(SearchKernel k) {
+      FLY_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, SEARCH_SMEM_CAP));
+    }
+  }  // namespace
+
   void search_init_kernels() {
-    static std::once_flag once;
-    std::call_once(once, [] {
-      for (bool mixed : {true, false})
-        for (int lpa : {1, 2, 4, 8})
-          for (SearchKernel k : kernels(mixed, lpa).k)
-            FLY_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, SEARCH_SMEM_CAP));
-    });
+    for (bool mixed : {true, false})
+      for (int lpa : {1, 2, 4, 8})
+        for (SearchKernel k : kernels(mixed, lpa).k) set_smem_cap(k);
   }
 
   void search_occupancy(int lanes_per_atom, int threads, bool mixed, int max_registers, int smem_bytes,
                         int* blocks_per_sm) {
-    search_init_kernels();
-    FLY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, pick(mixed, lanes_per_atom, max_registers),
-                                                           threads, static_cast<std::size_t>(smem_bytes)));
+    SearchKernel const k = pick(mixed, lanes_per_atom, max_registers);
+    set_smem_cap(k);
+    FLY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k, threads, static_cast<std::size_t>(smem_bytes)));
   }
 
   int search_smem_for(int lanes_per_atom, int threads, bool mixed, int max_registers, int blocks_per_sm, int need) {
@@ -169,8 +175,11 @@ namespace flygpu {
     if (threads % 32 != 0 || threads < 64 || threads > 1024)
       fail(FLYGPU_INVALID_ARG, "threads must be 64..1024, a multiple of 32");
     if (v.smem_bytes < 0 || v.smem_bytes > SEARCH_SMEM_CAP) fail(FLYGPU_INVALID_ARG, "search shared memory out of range");
-    search_init_kernels();
-    launch(pick(mixed, lanes_per_atom, max_registers), blocks, threads, static_cast<std::size_t>(v.smem_bytes), s, v);
+    SearchKernel const k = pick(mixed, lanes_per_atom, max_registers);
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    FLY_CUDA(cudaStreamIsCapturing(s, &cap));
+    if (cap == cudaStreamCaptureStatusNone) set_smem_cap(k);
+    launch(k, blocks, threads, static_cast<std::size_t>(v.smem_bytes), s, v);
   }
 
 }  // namespace flygpu

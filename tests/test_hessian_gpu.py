@@ -67,6 +67,22 @@ def test_hessian_bit_exact_vs_oracle(gpu, oracle, geam, odata, name, s, skin):
     assert np.array_equal(h, ref), np.abs(h - ref).max()
 
 
+def test_hessian_in_place_column_path_vs_oracle(gpu, oracle, geam, odata):
+    # 2420 atoms: a column block (3n rows of 3 doubles) no longer fits in one CTA's shared memory, so the
+    # column pass accumulates in place in the matrix; same contributions, same order, same bits
+    rng = np.random.default_rng(8)
+    pos = W.bcc_sites(11, 11, 10, W.A_FE) + rng.normal(0, 0.04, (2420, 3))
+    ext = np.array([11, 11, 10], float) * W.A_FE
+    centre = ext / 2
+    frozen = (np.linalg.norm(pos - centre, axis=1) > 5.0).astype(np.uint8)
+    assert 20 < int((frozen == 0).sum()) < 100
+    s = W.System(pos, np.zeros(2420, np.uint32), frozen, ext, np.ones(3, np.int32), {})
+    g, o = _pair(gpu, oracle, odata, s, odata.r_cut)
+    h = geam.hessian(s.types, s.frozen, g)
+    ref = oracle.eam_hessian(odata, o, s.types, s.frozen, threads=4)
+    assert np.array_equal(h, ref), np.abs(h - ref).max()
+
+
 @pytest.mark.parametrize("name,s,skin", _systems(), ids=lambda v: v if isinstance(v, str) else "")
 def test_mass_weighted_eigenvalues_vs_oracle(gpu, oracle, geam, odata, name, s, skin):
     g, o = _pair(gpu, oracle, odata, s, odata.r_cut + skin)
