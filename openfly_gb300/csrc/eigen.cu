@@ -279,6 +279,239 @@ namespace flygpu {
       cl.sync();  // no CTA leaves while another may still read its shared memory
     }
 
+    // ------------------------------------------------------------------ rows in shared memory, pushed
+    // The form used when every CTA's rows fit in its shared memory. Instead of reading row k, the p values
+    // and the shares across the cluster after each barrier, the producers write them into every CTA's
+    // shared memory before it: each warp pushes the p_i of its rows and its share of u^T p before the
+    // first barrier, and the owner of row k + 1 updates that row first, forms step k + 1's reflector u and
+    // tau from it with one warp, and pushes them (double-buffered by step parity) before the second. Every
+    // step then starts with u and tau local, and K and w need no remote reads. Values that several CTAs
+    // use (p_i, the shares, K) are formed by one lane and broadcast, so every CTA applies the same update.
+    //
+    // Shared memory (8-byte elements): rows R x M | u of even and odd steps 2 M | w M | p M |
+    // shares C * TW | tau of even and odd steps 2.
+
+    std::size_t tridiag_push_smem(int M, int C) {
+      std::size_t const R = static_cast<std::size_t>((M + C - 1) / C);
+      return (R * static_cast<std::size_t>(M) + 5 * static_cast<std::size_t>(M) + static_cast<std::size_t>(C) * TW + 2) *
+             sizeof(double);
+    }
+
+    // Sum over a warp of v, formed in lane 0's order and broadcast, so every lane (and every warp that
+    // sums the same values) holds the same bits.
+    __device__ inline ff warp_sum_bcast(ff v) {
+      for (int o = 16; o > 0; o >>= 1) v = ff_add(v, ff_shfl_down(v, o));
+      return {__shfl_sync(0xffffffffu, v.hi, 0), __shfl_sync(0xffffffffu, v.lo, 0)};
+    }
+
+    // The reflector's scalars from s2 = |x|^2 and x0 (every lane of a warp, the same values): alpha, tau
+    // and whether the column needs a reflection. The same operations as the cluster-wide form.
+    struct Refl {
+      ff alpha, tau;
+      bool reflect;
+    };
+    __device__ inline Refl reflector_scalars(ff s2, ff x0) {
+      float const sq = sqrtf(s2.hi);
+      ff nrm = {0.f, 0.f};
+      if (sq > 0.f) {
+        ff const r = ff_add(s2, ff_neg(ff_mul(ff{sq, 0.f}, ff{sq, 0.f})));
+        nrm = quick_two_sum(sq, __fdiv_rn(r.hi, 2.f * sq));
+      }
+      Refl o;
+      o.alpha = x0.hi > 0.f ? ff_neg(nrm) : nrm;
+      ff const den = ff_add(ff_mul(o.alpha, o.alpha), ff_neg(ff_mul(o.alpha, x0)));
+      o.reflect = den.hi > 0.f && ff_add(s2, ff_neg(ff_mul(x0, x0))).hi > 0.f;
+      o.tau = {0.f, 0.f};
+      if (o.reflect) {
+        float const r0 = __frcp_rn(den.hi);
+        ff const e1 = ff_add(ff{1.f, 0.f}, ff_neg(ff_mul(den, ff{r0, 0.f})));
+        o.tau = quick_two_sum(r0, __fmul_rn(r0, e1.hi));
+      }
+      return o;
+    }
+
+    // Lane 0 of the owner's warp: u[0], tau, d[s] and e[s] of step s (diag = A[s, s], x0 = A[s, s+1]).
+    __device__ inline void finish_reflector(Refl const& q, ff x0, ff diag, int s, ff* u, ff* tau, double* d, double* e) {
+      u[0] = q.reflect ? ff_add(x0, ff_neg(q.alpha)) : ff{0.f, 0.f};
+      *tau = q.tau;
+      d[s] = ff_dbl(diag);
+      e[s] = ff_dbl(q.reflect ? q.alpha : x0);
+    }
+
+    // One warp of the owner of row s: the reflector of step s from x = A[s, s+1:] (row points at row s),
+    // u into u (M - s - 1 values) and tau into *tau; d[s] = A[s, s] and e[s] = alpha (x0 when the column
+    // needs no reflection).
+    __device__ void form_reflector(ff const* row, int s, int M, ff* u, ff* tau, double* d, double* e) {
+      int const lane = threadIdx.x & 31;
+      int const b = s + 1, m = M - b;
+      ff s2 = {0.f, 0.f};
+      for (int j = lane; j < m; j += 32) {
+        ff const x = row[b + j];
+        u[j] = x;
+        s2 = ff_add(s2, ff_mul(x, x));
+      }
+      s2 = warp_sum_bcast(s2);
+      ff const x0 = row[b];
+      Refl const q = reflector_scalars(s2, x0);
+      __syncwarp();
+      if (lane == 0) finish_reflector(q, x0, row[s], s, u, tau, d, e);
+      __syncwarp();
+    }
+
+    // The owner's warp 0 at step k (row b = k + 1, ri = row b from column b, m = M - b): updates row b and,
+    // in the same pass, gathers step k + 1's x = A[b, b+1:] into un and its |x|^2; then the reflector.
+    __device__ void update_and_reflect(ff* ri, ff ui, ff wi, ff const* u, ff const* w, int m, int b, ff* un,
+                                       ff* tau, double* d, double* e) {
+      int const lane = threadIdx.x & 31;
+      ff s2 = {0.f, 0.f};
+      for (int j = lane; j < m; j += 32) {
+        ff const v = ff_add(ri[j], ff_neg(ff_add(ff_mul(ui, w[j]), ff_mul(wi, u[j]))));
+        ri[j] = v;
+        if (j >= 1) {
+          un[j - 1] = v;
+          s2 = ff_add(s2, ff_mul(v, v));
+        }
+      }
+      s2 = warp_sum_bcast(s2);
+      __syncwarp();
+      ff const x0 = ri[1];
+      Refl const q = reflector_scalars(s2, x0);
+      __syncwarp();
+      if (lane == 0) finish_reflector(q, x0, ri[0], b, un, tau, d, e);
+      __syncwarp();
+    }
+
+    // Row update A_ij -= u_i w_j + w_i u_j over j < m (ri points at column b of row i), one warp.
+    __device__ inline void update_row(ff* ri, ff ui, ff wi, ff const* u, ff const* w, int m) {
+      int const lane = threadIdx.x & 31;
+      int j = lane;
+      for (; j + 96 < m; j += 128) {
+        ff v[4];
+#pragma unroll
+        for (int t = 0; t < 4; ++t) v[t] = ri[j + 32 * t];
+#pragma unroll
+        for (int t = 0; t < 4; ++t)
+          ri[j + 32 * t] = ff_add(v[t], ff_neg(ff_add(ff_mul(ui, w[j + 32 * t]), ff_mul(wi, u[j + 32 * t]))));
+      }
+      for (; j < m; j += 32) ri[j] = ff_add(ri[j], ff_neg(ff_add(ff_mul(ui, w[j]), ff_mul(wi, u[j]))));
+    }
+
+    // One warp of the owner copies step s's u (m values) and tau from its shared memory into every other
+    // CTA's.
+    __device__ inline void push_reflector(cg::cluster_group& cl, ff const* u, ff const* tau, int m) {
+      int const C = static_cast<int>(cl.num_blocks()), c = static_cast<int>(cl.block_rank());
+      int const lane = threadIdx.x & 31;
+      for (int dst = 0; dst < C; ++dst) {
+        if (dst == c) continue;
+        ff* const ru = cl.map_shared_rank(const_cast<ff*>(u), dst);
+        for (int j = lane; j < m; j += 32) ru[j] = u[j];
+      }
+      if (lane < C && lane != c) *cl.map_shared_rank(const_cast<ff*>(tau), lane) = *tau;
+    }
+
+    // The whole owner CTA copies step s's u (m values) and tau into every other CTA's shared memory.
+    __device__ inline void push_reflector_cta(cg::cluster_group& cl, ff const* u, ff const* tau, int m) {
+      int const C = static_cast<int>(cl.num_blocks()), c = static_cast<int>(cl.block_rank());
+      for (int dst = 0; dst < C; ++dst) {
+        if (dst == c) continue;
+        ff* const ru = cl.map_shared_rank(const_cast<ff*>(u), dst);
+        for (int j = threadIdx.x; j < m; j += TT) ru[j] = u[j];
+      }
+      if (static_cast<int>(threadIdx.x) < C && static_cast<int>(threadIdx.x) != c)
+        *cl.map_shared_rank(const_cast<ff*>(tau), threadIdx.x) = *tau;
+    }
+
+    __global__ void __launch_bounds__(TT) k_tridiag_push(double const* __restrict__ A, int M, double* __restrict__ d,
+                                                        double* __restrict__ e) {
+      cg::cluster_group cl = cg::this_cluster();
+      int const C = static_cast<int>(cl.num_blocks());
+      int const c = static_cast<int>(cl.block_rank());
+      int const R = (M + C - 1) / C;
+      extern __shared__ ff sm[];
+      ff* const rows = sm;                                        // R x M: row r * C + c at rows + r M
+      ff* const ub = rows + static_cast<std::int64_t>(R) * M;     // 2 M
+      ff* const w = ub + 2 * M;                                   // M
+      ff* const pa = w + M;                                       // M: p_i of every row
+      ff* const shs = pa + M;                                     // C * TW
+      ff* const tb = shs + C * TW;                                // 2
+      int const lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+      for (int r = warp; r * C + c < M; r += TW)
+        for (int j = lane; j < M; j += 32)
+          rows[static_cast<std::int64_t>(r) * M + j] = ff_of(__ldcg(A + static_cast<std::int64_t>(r * C + c) * M + j));
+      cl.sync();  // every CTA runs, so its shared memory may be written
+      if (M >= 3 && c == 0 && warp == 0) {  // step 0's reflector, from row 0
+        form_reflector(rows, 0, M, ub, tb, d, e);
+        push_reflector(cl, ub, tb, M - 1);
+      }
+      cl.sync();
+      for (int k = 0; k + 2 < M; ++k) {
+        int const b = k + 1, m = M - b, cb = k & 1;
+        ff const* const u = ub + cb * M;
+        ff const tau = tb[cb];
+        int const r0 = (b - c + C - 1) / C;  // the first owned row at or below row b
+        // p_i = tau (A u)_i of the owned rows, pushed to every CTA, and the warp's share of u^T p
+        ff sh = {0.f, 0.f};
+        for (int r = r0 + warp; r < R && r * C + c < M; r += TW) {
+          int const i = r * C + c;
+          ff const* ri = rows + static_cast<std::int64_t>(r) * M + b;
+          ff acc[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+          int j = lane;
+          for (; j + 96 < m; j += 128) {
+            ff v[4];
+#pragma unroll
+            for (int t = 0; t < 4; ++t) v[t] = ri[j + 32 * t];
+#pragma unroll
+            for (int t = 0; t < 4; ++t) acc[t] = ff_add(acc[t], ff_mul(v[t], u[j + 32 * t]));
+          }
+          for (; j < m; j += 32) acc[0] = ff_add(acc[0], ff_mul(ri[j], u[j]));
+          ff const a = warp_sum_bcast(ff_add(ff_add(acc[0], acc[1]), ff_add(acc[2], acc[3])));
+          ff const pi = ff_mul(tau, a);
+          if (lane < C) *cl.map_shared_rank(pa + i, lane) = pi;
+          sh = ff_add(sh, ff_mul(u[i - b], pi));
+        }
+        if (lane < C) cl.map_shared_rank(shs, lane)[c * TW + warp] = sh;
+        cl.sync();
+        // K = tau / 2 sum of every warp's share: the same order in every warp of every CTA
+        ff t = {0.f, 0.f};
+        for (int q = lane; q < C * TW; q += 32) t = ff_add(t, shs[q]);
+        ff const K = ff_mul(ff_mul(tau, warp_sum_bcast(t)), ff{0.5f, 0.f});
+        for (int j = threadIdx.x; j < m; j += TT) w[j] = ff_add(pa[b + j], ff_neg(ff_mul(K, u[j])));
+        __syncthreads();
+        bool const next = k + 3 < M;  // a step k + 1 follows
+        if (c == b % C) {
+          // this CTA owns row b: warp 0 updates it and forms step k + 1's reflector from it while the
+          // other warps update the remaining rows; then the whole CTA pushes the reflector
+          if (warp == 0) {
+            ff* const rb = rows + static_cast<std::int64_t>(r0) * M + b;
+            if (next) update_and_reflect(rb, u[0], w[0], u, w, m, b, ub + (cb ^ 1) * M, tb + (cb ^ 1), d, e);
+            else update_row(rb, u[0], w[0], u, w, m);
+          } else {
+            for (int r = r0 + warp; r < R && r * C + c < M; r += TW - 1) {
+              int const i = r * C + c;
+              update_row(rows + static_cast<std::int64_t>(r) * M + b, u[i - b], w[i - b], u, w, m);
+            }
+          }
+          __syncthreads();
+          if (next) push_reflector_cta(cl, ub + (cb ^ 1) * M, tb + (cb ^ 1), m - 1);
+        } else {
+          for (int r = r0 + warp; r < R && r * C + c < M; r += TW) {
+            int const i = r * C + c;
+            update_row(rows + static_cast<std::int64_t>(r) * M + b, u[i - b], w[i - b], u, w, m);
+          }
+        }
+        cl.sync();
+      }
+      if (c == 0 && threadIdx.x == 0) {
+        auto at = [&](int i, int j) { return ff_dbl(cl.map_shared_rank(rows, i % C)[static_cast<std::int64_t>(i / C) * M + j]); };
+        if (M >= 2) {
+          d[M - 2] = at(M - 2, M - 2);
+          e[M - 2] = at(M - 1, M - 2);
+        }
+        d[M - 1] = at(M - 1, M - 1);
+      }
+      cl.sync();  // no CTA leaves while another may still read its shared memory
+    }
+
     // Number of eigenvalues of the tridiagonal (d, e2 = e^2, as float-float) below x: the sign changes
     // of the sequence 1, p_0, p_1, ... of leading principal minors of T - x I,
     // p_i = (d_i - x) p_{i-1} - e_{i-1}^2 p_{i-2} (the Sturm sequence), in float-float arithmetic on the
@@ -336,6 +569,51 @@ namespace flygpu {
       if (lane == 0) eig[j] = 0.5 * (lo + hi);
     }
 
+    // The multisection's inputs from the tridiagonal (d, e; one CTA): d and e^2 as float-float, and
+    // bounds = {lo, hi, tol, flag}: the Gershgorin interval of T padded by 2 eps |T| M, the stopping width
+    // 2 eps |T|, and flag = 1 when |T| is beyond the float-float range.
+    constexpr int PREP_T = 1024;
+    __global__ void __launch_bounds__(PREP_T) k_tri_prep(double const* __restrict__ d, double const* __restrict__ e, int M,
+                                                        ff* __restrict__ dff, ff* __restrict__ e2ff,
+                                                        double* __restrict__ bounds) {
+      __shared__ double red[3][PREP_T / 32];
+      int const lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+      double lo = INFINITY, hi = -INFINITY, tn = 0;
+      for (int i = threadIdx.x; i < M; i += PREP_T) {
+        double const el = i > 0 ? fabs(e[i - 1]) : 0.0;
+        double const er = i + 1 < M ? fabs(e[i]) : 0.0;
+        double const a = d[i];
+        lo = fmin(lo, a - el - er);
+        hi = fmax(hi, a + el + er);
+        tn = fmax(tn, fabs(a) + el + er);
+        dff[i] = ff_of(a);
+        e2ff[i] = i + 1 < M ? ff_of(e[i] * e[i]) : ff{0.f, 0.f};
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        lo = fmin(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+        hi = fmax(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+        tn = fmax(tn, __shfl_xor_sync(0xffffffffu, tn, o));
+      }
+      if (lane == 0) {
+        red[0][warp] = lo;
+        red[1][warp] = hi;
+        red[2][warp] = tn;
+      }
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        for (int w = 1; w < PREP_T / 32; ++w) {
+          lo = fmin(lo, red[0][w]);
+          hi = fmax(hi, red[1][w]);
+          tn = fmax(tn, red[2][w]);
+        }
+        double const pad = 2 * DBL_EPSILON * fmax(tn, DBL_MIN) * static_cast<double>(M) + DBL_MIN;
+        bounds[0] = lo - pad;
+        bounds[1] = hi + pad;
+        bounds[2] = 2 * DBL_EPSILON * tn;
+        bounds[3] = tn < 1e18 ? 0.0 : 1.0;
+      }
+    }
+
     // out (M x M, full) = the symmetric matrix of the row-major lower triangle of H (N x N) restricted to
     // the coordinates act (all when act is null).
     __global__ void k_sym_gather(double const* __restrict__ H, std::int64_t N, int const* __restrict__ act,
@@ -367,35 +645,38 @@ namespace flygpu {
       return cfg;
     }
 
-    template <bool SM>
-    bool tridiag_fits(int M, int C) {
-      std::size_t const smem = tridiag_smem(M, C, SM);
+    // Whether a cluster of C CTAs of kernel k with smem bytes each can run on this device.
+    template <class K>
+    bool cluster_fits(K k, int C, std::size_t smem) {
       if (smem > static_cast<std::size_t>(TRIDIAG_SMEM_MAX)) return false;
       cudaLaunchAttribute at{};
       cudaLaunchConfig_t const cfg = tridiag_config(C, smem, at, nullptr);
       int n = 0;
-      bool const ok = cudaOccupancyMaxActiveClusters(&n, k_tridiag<SM>, &cfg) == cudaSuccess && n > 0;
+      bool const ok = cudaOccupancyMaxActiveClusters(&n, k, &cfg) == cudaSuccess && n > 0;
       cudaGetLastError();
       return ok;
     }
 
     // Launches the tridiagonalisation of the M x M matrix A (global) on stream s: the largest cluster
-    // (16, 8, ... CTAs) the device can hold, with the rows in shared memory when they fit. The kernels'
-    // shared-memory limits are set to the same constant on every call, so concurrent callers agree.
+    // (16, 8, ... CTAs) the device can hold, with the rows in shared memory (k_tridiag_push) when they fit,
+    // else in the global matrix. The kernels' shared-memory limits are set to the same constant on every
+    // call, so concurrent callers agree.
     void tridiag_launch(double* A, int M, double* d, double* e, cudaStream_t s) {
-      for (auto k : {k_tridiag<true>, k_tridiag<false>}) {
-        FLY_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, TRIDIAG_SMEM_MAX));
-        FLY_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
-      }
-      for (int C : {16, 8, 4, 2, 1}) {
-        bool const sm = tridiag_fits<true>(M, C);
-        if (!sm && !tridiag_fits<false>(M, C)) continue;
+      FLY_CUDA(cudaFuncSetAttribute(k_tridiag_push, cudaFuncAttributeMaxDynamicSharedMemorySize, TRIDIAG_SMEM_MAX));
+      FLY_CUDA(cudaFuncSetAttribute(k_tridiag_push, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+      FLY_CUDA(cudaFuncSetAttribute(k_tridiag<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, TRIDIAG_SMEM_MAX));
+      FLY_CUDA(cudaFuncSetAttribute(k_tridiag<false>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+      for (int C : {8, 16, 4, 2, 1}) {
+        std::size_t const sp = tridiag_push_smem(M, C), sg = tridiag_smem(M, C, false);
         cudaLaunchAttribute at{};
-        cudaLaunchConfig_t const cfg = tridiag_config(C, tridiag_smem(M, C, sm), at, s);
-        if (sm) {
-          FLY_CUDA(cudaLaunchKernelEx(&cfg, k_tridiag<true>, A, M, d, e));
-        } else {
+        if (cluster_fits(k_tridiag_push, C, sp)) {
+          cudaLaunchConfig_t const cfg = tridiag_config(C, sp, at, s);
+          FLY_CUDA(cudaLaunchKernelEx(&cfg, k_tridiag_push, static_cast<double const*>(A), M, d, e));
+        } else if (cluster_fits(k_tridiag<false>, C, sg)) {
+          cudaLaunchConfig_t const cfg = tridiag_config(C, sg, at, s);
           FLY_CUDA(cudaLaunchKernelEx(&cfg, k_tridiag<false>, A, M, d, e));
+        } else {
+          continue;
         }
         count_launch();
         return;
@@ -425,47 +706,21 @@ namespace flygpu {
     double* const ee = dd + M;
     double* const fb = ee + M;   // 2 M: d and e^2 as float-float (4 M floats)
     double* const ww = fb + 2 * M;
-    double* const bnd = ww + M;  // 3
+    double* const bnd = ww + M;  // 4
     int const Mi = static_cast<int>(M);
     tridiag_launch(P.sub.p, Mi, dd, ee, s);
-    // Gershgorin interval and stopping width on the host (O(M) values)
-    std::vector<double> hd(static_cast<std::size_t>(M)), he(static_cast<std::size_t>(M));
-    FLY_CUDA(cudaMemcpyAsync(hd.data(), dd, sizeof(double) * hd.size(), cudaMemcpyDeviceToHost, s));
-    FLY_CUDA(cudaMemcpyAsync(he.data(), ee, sizeof(double) * he.size(), cudaMemcpyDeviceToHost, s));
-    FLY_CUDA(cudaStreamSynchronize(s));
-    std::vector<double> he2(static_cast<std::size_t>(M), 0.0);
-    double lo = 0, hi = 0, tnorm = 0;
-    for (std::int64_t i = 0; i < M; ++i) {
-      std::size_t const k = static_cast<std::size_t>(i);
-      double const el = i > 0 ? std::fabs(he[k - 1]) : 0.0;
-      double const er = i + 1 < M ? std::fabs(he[k]) : 0.0;
-      double const a = hd[k];
-      lo = i == 0 ? a - el - er : std::min(lo, a - el - er);
-      hi = i == 0 ? a + el + er : std::max(hi, a + el + er);
-      tnorm = std::max(tnorm, std::fabs(a) + el + er);
-      if (i + 1 < M) he2[k] = he[k] * he[k];
-    }
-    if (!(tnorm < 1e18)) fail(FLYGPU_INVALID_ARG, "matrix norm beyond the eigensolver's float-float range");
-    double const pad = 2 * DBL_EPSILON * std::max(tnorm, DBL_MIN) * static_cast<double>(M) + DBL_MIN;
-    double const hb[3] = {lo - pad, hi + pad, 2 * DBL_EPSILON * tnorm};
-    // d and e^2 as float-float pairs (hi, lo) for the multisection
-    std::vector<float> hff(4 * static_cast<std::size_t>(M));
-    for (std::int64_t i = 0; i < M; ++i) {
-      std::size_t const k = static_cast<std::size_t>(i);
-      float const dh = static_cast<float>(hd[k]), eh = static_cast<float>(he2[k]);
-      hff[2 * k] = dh;
-      hff[2 * k + 1] = static_cast<float>(hd[k] - static_cast<double>(dh));
-      hff[2 * static_cast<std::size_t>(M) + 2 * k] = eh;
-      hff[2 * static_cast<std::size_t>(M) + 2 * k + 1] = static_cast<float>(he2[k] - static_cast<double>(eh));
-    }
+    // d and e^2 as float-float pairs, the Gershgorin interval and the stopping width, on the device
     ff* const dff = reinterpret_cast<ff*>(fb);
-    FLY_CUDA(cudaMemcpyAsync(dff, hff.data(), sizeof(float) * hff.size(), cudaMemcpyHostToDevice, s));
-    FLY_CUDA(cudaMemcpyAsync(bnd, hb, sizeof hb, cudaMemcpyHostToDevice, s));
+    launch(k_tri_prep, 1, PREP_T, 0, s, static_cast<double const*>(dd), static_cast<double const*>(ee), Mi, dff, dff + M,
+           bnd);
     // one warp per block: the warps spread over every SM
     launch(k_bisect, static_cast<unsigned>(M), 32, 0, s, static_cast<ff const*>(dff), static_cast<ff const*>(dff + M), Mi,
            static_cast<double const*>(bnd), ww);
+    double flag = 0;
     FLY_CUDA(cudaMemcpyAsync(h_eig, ww, sizeof(double) * static_cast<std::size_t>(M), cudaMemcpyDeviceToHost, s));
+    FLY_CUDA(cudaMemcpyAsync(&flag, bnd + 3, sizeof(double), cudaMemcpyDeviceToHost, s));
     FLY_CUDA(cudaStreamSynchronize(s));
+    if (flag != 0) fail(FLYGPU_INVALID_ARG, "matrix norm beyond the eigensolver's float-float range");
   }
 
 }  // namespace flygpu

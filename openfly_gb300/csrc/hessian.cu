@@ -524,7 +524,9 @@ namespace flygpu {
 
   }  // namespace
 
-  // Dense 3n x 3n Hessian into d_H (device, row-major). Synchronises the list's stream.
+  // Dense 3n x 3n Hessian into d_H (device, row-major), on the list's stream. Waits for the list export's
+  // pair counts; the Hessian kernels run on after the return (host data is copied from pageable memory,
+  // which the driver stages before the copy call returns).
   void eam_hessian(flygpu_eam const* E, flygpu_list* L, std::uint8_t const* h_frozen, double* d_H) {
     std::int64_t const n = L->n;
     cudaStream_t const s = L->stream;
@@ -541,17 +543,15 @@ namespace flygpu {
     P.cols.reserve(std::max<std::size_t>(cols.size(), 1));
     if (!cols.empty())
       FLY_CUDA(cudaMemcpyAsync(P.cols.p, cols.data(), sizeof(int) * cols.size(), cudaMemcpyHostToDevice, s));
-    P.offs.reserve(static_cast<std::size_t>(n) + 1);
     std::vector<int> const cnt = list_export_device(L, E->r_cut, P.offs, P.idx, P.dr);
-    std::vector<long long> ho(static_cast<std::size_t>(n) + 1, 0);
-    for (std::int64_t i = 0; i < n; ++i) ho[static_cast<std::size_t>(i) + 1] = ho[static_cast<std::size_t>(i)] + cnt[static_cast<std::size_t>(i)];
-    FLY_CUDA(cudaMemcpyAsync(P.offs.p, ho.data(), sizeof(long long) * ho.size(), cudaMemcpyHostToDevice, s));
+    long long n_pairs_ll = 0;
+    for (int const c : cnt) n_pairs_ll += c;
     P.rho_mu.reserve(4 * static_cast<std::size_t>(n));
     P.fder.reserve(2 * static_cast<std::size_t>(n));
     std::size_t const N = 3 * static_cast<std::size_t>(n);
     FLY_CUDA(cudaMemsetAsync(d_H, 0, sizeof(double) * N * N, s));
     TablesView const tb = E->view();
-    std::size_t const n_pairs = static_cast<std::size_t>(ho.back());
+    std::size_t const n_pairs = static_cast<std::size_t>(n_pairs_ll);
     P.pr.reserve(std::max<std::size_t>(n_pairs, 1));
     P.pfp.reserve(std::max<std::size_t>(n_pairs, 1));
     P.key.reserve(std::max<std::size_t>(n_pairs, 1));
@@ -571,7 +571,6 @@ namespace flygpu {
       launch(k_hess_col, static_cast<unsigned>(cols.size()), COL_T, smem, s, tb, n, P.cols.p, P.offs.p, P.idx.p,
              P.dr.p, L->types.p, L->frozen.p, P.rho_mu.p, P.fder.p, P.pr.p, P.pfp.p, P.key.p, d_H, in_smem, L->err.p);
     }
-    FLY_CUDA(cudaStreamSynchronize(s));  // the host vectors ho and cols stay alive until their copies have run
   }
 
   void hessian_mass_weight(flygpu_eam const* E, flygpu_list* L, double const* type_mass, std::uint32_t const* h_types,
@@ -604,7 +603,6 @@ namespace flygpu {
     unsigned const gx = static_cast<unsigned>(std::min<std::int64_t>((N + 255) / 256, 64));
     unsigned const gy = static_cast<unsigned>(std::min<std::int64_t>(N, 65535));
     launch(k_mass_weight, dim3(gx, gy), 256, 0, s, d_H, N, dt.p, dm.p + nt, nt);
-    FLY_CUDA(cudaStreamSynchronize(s));
   }
 
   // Eigenvalues of a Hessian whose frozen atoms' rows and columns are zero: the matrix is block diagonal

@@ -276,8 +276,9 @@ namespace flygpu {
   void list_rebuild(flygpu_list* L, double const* d_pos, std::int64_t n);
   void list_update(flygpu_list* L, double const* d_delta);
   // For each real atom (reference index) its neighbours within r_cut in the list's order, on the device:
-  // offs[i] = first entry of atom i, idx (reference indices) and dr (xyz, binary64 r_n - r_i). Returns
-  // the per-atom counts on the host. Synchronises the list's stream.
+  // offs[i] = first entry of atom i (n + 1 entries, offs[n] = the total), idx (reference indices) and dr
+  // (xyz, binary64 r_n - r_i). Returns the per-atom counts on the host: waits for the counting pass; the
+  // filling pass runs on after the return, on the list's stream.
   std::vector<int> list_export_device(flygpu_list* L, double r_cut, DevBuf<long long>& offs, DevBuf<int>& idx,
                                       DevBuf<double>& dr);
   // One real atom's neighbours within r_cut in List::for_neighbours order: real indices and binary64

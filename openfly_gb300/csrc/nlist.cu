@@ -687,20 +687,21 @@ namespace flygpu {
            d_counts.p);
     FLY_CUDA(cudaMemcpyAsync(hc.data(), d_counts.p, sizeof(int) * hc.size(), cudaMemcpyDeviceToHost, s));
     FLY_CUDA(cudaStreamSynchronize(s));
-    std::vector<long long> ho(static_cast<std::size_t>(n));
+    std::vector<long long> ho(static_cast<std::size_t>(n) + 1);
     long long total = 0;
     for (std::int64_t i = 0; i < n; ++i) {
       ho[static_cast<std::size_t>(i)] = total;
       total += hc[static_cast<std::size_t>(i)];
     }
-    offs.reserve(static_cast<std::size_t>(n));
+    ho[static_cast<std::size_t>(n)] = total;
+    offs.reserve(static_cast<std::size_t>(n) + 1);
     idx.reserve(static_cast<std::size_t>(std::max<long long>(total, 1)));
     dr.reserve(static_cast<std::size_t>(3 * std::max<long long>(total, 1)));
+    // a copy from pageable memory returns once the driver has staged it, so ho may go out of scope
     FLY_CUDA(cudaMemcpyAsync(offs.p, ho.data(), sizeof(long long) * ho.size(), cudaMemcpyHostToDevice, s));
     if (total > 0)
       launch(k_export_fill, blocks_for(n), T, 0, s, L->pos.p, L->real_phys.p, L->pimg.p, L->nbr.p, L->ncount.p, n, rc2,
              offs.p, idx.p, dr.p);
-    FLY_CUDA(cudaStreamSynchronize(s));
     return hc;
   }
 
