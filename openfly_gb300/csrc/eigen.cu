@@ -542,27 +542,67 @@ namespace flygpu {
       return cnt;
     }
 
-    // One warp per eigenvalue index; bounds = {lo, hi, tol} (binary64).
-    __global__ void k_bisect(ff const* __restrict__ d, ff const* __restrict__ e2, int M,
-                             double const* __restrict__ bounds, double* __restrict__ eig) {
+    // The same count in binary32 (the high parts of d and e^2). It is the exact count of a tridiagonal
+    // within about 8 eps32 |T| of T (each step's rounding perturbs d_i - x and e_{i-1}^2 relatively by a
+    // few eps32, and the rounding of the data and of x adds eps32 |T|): so a count of more than j at x
+    // puts eigenvalue j below x + delta, and a count of at most j puts it at or above x - delta, for the
+    // delta that k_tri_prep supplies (32 eps32 |T|).
+    __device__ int sturm_count32(ff const* __restrict__ d, ff const* __restrict__ e2, int M, float x) {
+      float pm = 1.f;
+      float p = __fsub_rn(d[0].hi, x);
+      if (p == 0.f) p = -0x1p-40f;
+      int cnt = p < 0.f;
+      for (int i = 1; i < M; ++i) {
+        float pn = fmaf(__fsub_rn(d[i].hi, x), p, -__fmul_rn(e2[i - 1].hi, pm));
+        if (pn == 0.f) pn = -p * 0x1p-40f;
+        cnt += (pn < 0.f) != (p < 0.f);
+        pm = p;
+        p = pn;
+        float const ap = fabsf(p);
+        if (ap > 0x1p60f) {
+          p *= 0x1p-64f;
+          pm *= 0x1p-64f;
+        } else if (ap < 0x1p-60f && fabsf(pm) < 0x1p-60f) {
+          p *= 0x1p64f;
+          pm *= 0x1p64f;
+        }
+      }
+      return cnt;
+    }
+
+    // One warp per eigenvalue index j; bounds = {lo, hi, tol, flag, delta} (binary64). Each round the 32
+    // lanes count the eigenvalues below 32 points that split the interval into 33 equal parts, and the
+    // interval becomes the part holding eigenvalue j. The rounds run in binary32 (a recurrence step a
+    // quarter as long) while the interval is wider than 16 delta; the interval is then widened by delta
+    // on both sides, which keeps eigenvalue j inside it, and the float-float rounds finish it.
+    __global__ void __launch_bounds__(32) k_bisect(ff const* __restrict__ d, ff const* __restrict__ e2, int M,
+                                                  double const* __restrict__ bounds, double* __restrict__ eig) {
       int const lane = threadIdx.x & 31;
-      int const j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-      if (j >= M) return;
+      int const j = blockIdx.x;
       double lo = bounds[0], hi = bounds[1];
-      double const tol = bounds[2];
-      for (int it = 0; it < 64; ++it) {
+      double const tol = bounds[2], delta = bounds[4];
+      bool fast = true;
+      for (int it = 0; it < 96; ++it) {
         double const width = hi - lo;
-        if (width <= fmax(tol, 4 * DBL_EPSILON * fmax(fabs(lo), fabs(hi)))) break;
-        double const x = lo + width * (static_cast<double>(lane + 1) * (1.0 / 33.0));
-        int const cnt = sturm_count(d, e2, M, ff_of(x));
+        if (fast && !(width > 16 * delta)) {
+          fast = false;
+          lo -= delta;
+          hi += delta;
+          continue;
+        }
+        if (!fast && width <= fmax(tol, 4 * DBL_EPSILON * fmax(fabs(lo), fabs(hi)))) break;
+        double const step = width * (1.0 / 33.0);
+        double const x = lo + step * static_cast<double>(lane + 1);
+        int const cnt = fast ? sturm_count32(d, e2, M, __double2float_rn(x)) : sturm_count(d, e2, M, ff_of(x));
         unsigned const above = __ballot_sync(0xffffffffu, cnt > j);
-        double const xs = __shfl_sync(0xffffffffu, x, above ? __ffs(above) - 1 : 31);
-        if (above == 0u) {
-          lo = xs;
+        int const f = above ? __ffs(above) - 1 : 32;  // the first point with more than j below it
+        // the same expression as x for points f - 1 and f
+        double const xf = lo + step * static_cast<double>(f + 1);
+        double const xp = lo + step * static_cast<double>(f);
+        if (f == 32) {
+          lo = xp;
         } else {
-          int const f = __ffs(above) - 1;
-          double const xp = __shfl_sync(0xffffffffu, x, f > 0 ? f - 1 : 0);
-          hi = xs;
+          hi = xf;
           if (f > 0) lo = xp;
         }
       }
@@ -570,8 +610,9 @@ namespace flygpu {
     }
 
     // The multisection's inputs from the tridiagonal (d, e; one CTA): d and e^2 as float-float, and
-    // bounds = {lo, hi, tol, flag}: the Gershgorin interval of T padded by 2 eps |T| M, the stopping width
-    // 2 eps |T|, and flag = 1 when |T| is beyond the float-float range.
+    // bounds = {lo, hi, tol, flag, delta}: the Gershgorin interval of T padded by 2 eps |T| M, the stopping
+    // width 2 eps |T|, flag = 1 when |T| >= 2^30 (the recurrences' products e^2 p stay inside binary32's range
+    // below that: p is kept within 2^-60 .. 2^60), and delta = 32 eps32 |T|.
     constexpr int PREP_T = 1024;
     __global__ void __launch_bounds__(PREP_T) k_tri_prep(double const* __restrict__ d, double const* __restrict__ e, int M,
                                                         ff* __restrict__ dff, ff* __restrict__ e2ff,
@@ -610,7 +651,8 @@ namespace flygpu {
         bounds[0] = lo - pad;
         bounds[1] = hi + pad;
         bounds[2] = 2 * DBL_EPSILON * tn;
-        bounds[3] = tn < 1e18 ? 0.0 : 1.0;
+        bounds[3] = tn < 0x1p30 ? 0.0 : 1.0;
+        bounds[4] = 32 * 0x1p-24 * tn;  // the binary32 counts' reach (k_bisect)
       }
     }
 
@@ -706,7 +748,7 @@ namespace flygpu {
     double* const ee = dd + M;
     double* const fb = ee + M;   // 2 M: d and e^2 as float-float (4 M floats)
     double* const ww = fb + 2 * M;
-    double* const bnd = ww + M;  // 4
+    double* const bnd = ww + M;  // 5
     int const Mi = static_cast<int>(M);
     tridiag_launch(P.sub.p, Mi, dd, ee, s);
     // d and e^2 as float-float pairs, the Gershgorin interval and the stopping width, on the device

@@ -335,7 +335,20 @@ namespace flygpu {
       int const p = real_phys[j];
       D4 const ri = pos[p];
       int c = 0;
-      for (int k = 0; k < ncount[j]; ++k) {
+      int const nc = ncount[j];
+      int k = 0;
+      // four neighbours' loads in flight together
+      for (; k + 4 <= nc; k += 4) {
+        D4 rq[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) rq[u] = pos[nbr[static_cast<std::int64_t>(k + u) * n + j]];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          double const dx = rq[u].x - ri.x, dy = rq[u].y - ri.y, dz = rq[u].z - ri.z;
+          if ((dx * dx + dy * dy) + dz * dz < rc2) ++c;
+        }
+      }
+      for (; k < nc; ++k) {
         D4 const rq = pos[nbr[static_cast<std::int64_t>(k) * n + j]];
         double const dx = rq.x - ri.x, dy = rq.y - ri.y, dz = rq.z - ri.z;
         if ((dx * dx + dy * dy) + dz * dz < rc2) ++c;
@@ -380,7 +393,32 @@ namespace flygpu {
       int const p = real_phys[j];
       D4 const ri = pos[p];
       long long o = offs[pimg[p]];
-      for (int k = 0; k < ncount[j]; ++k) {
+      int const nc = ncount[j];
+      int k = 0;
+      // four neighbours' loads in flight together, written in list order
+      for (; k + 4 <= nc; k += 4) {
+        int q[4], im[4];
+        D4 rq[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) q[u] = nbr[static_cast<std::int64_t>(k + u) * n + j];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          rq[u] = pos[q[u]];
+          im[u] = pimg[q[u]];
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          double const dx = rq[u].x - ri.x, dy = rq[u].y - ri.y, dz = rq[u].z - ri.z;
+          if ((dx * dx + dy * dy) + dz * dz < rc2) {
+            idx[o] = im[u];
+            dr[3 * o + 0] = dx;
+            dr[3 * o + 1] = dy;
+            dr[3 * o + 2] = dz;
+            ++o;
+          }
+        }
+      }
+      for (; k < nc; ++k) {
         int const q = nbr[static_cast<std::int64_t>(k) * n + j];
         D4 const rq = pos[q];
         double const dx = rq.x - ri.x, dy = rq.y - ri.y, dz = rq.z - ri.z;
