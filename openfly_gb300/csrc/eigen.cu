@@ -82,6 +82,40 @@ namespace flygpu {
       return {__shfl_xor_sync(0xffffffffu, a.hi, o), __shfl_xor_sync(0xffffffffu, a.lo, o)};
     }
 
+    // The same arithmetic with fewer renormalisations, for the tridiagonalisation's inner loops. A product
+    // a b as the unnormalised pair p + e (exact but for a.lo b.lo), TwoSum, a dot-product step that keeps
+    // its accumulator unnormalised, and the row update v - (a b + c d).
+    __device__ inline void ff_prod(ff a, ff b, float& p, float& e) {
+      p = __fmul_rn(a.hi, b.hi);
+      e = fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, fmaf(a.hi, b.hi, -p)));
+    }
+    __device__ inline void two_sum(float a, float b, float& s, float& err) {
+      s = __fadd_rn(a, b);
+      float const bb = __fsub_rn(s, a);
+      err = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+    }
+    __device__ inline void ff_dot_step(ff& acc, ff a, ff b) {  // acc += a b, acc.lo left unnormalised
+      float p, e, s, err;
+      ff_prod(a, b, p, e);
+      two_sum(acc.hi, p, s, err);
+      acc.hi = s;
+      acc.lo = __fadd_rn(acc.lo, __fadd_rn(e, err));
+    }
+    __device__ inline ff ff_norm(ff a) {  // an unnormalised pair as a float-float value
+      float s, err;
+      two_sum(a.hi, a.lo, s, err);
+      return {s, err};
+    }
+    __device__ inline ff ff_sub_dot2(ff v, ff a, ff b, ff c, ff d) {  // v - (a b + c d)
+      float p1, e1, p2, e2, s, err, s2, err2;
+      ff_prod(a, b, p1, e1);
+      ff_prod(c, d, p2, e2);
+      two_sum(p1, p2, s, err);
+      float const t = __fadd_rn(__fadd_rn(e1, e2), err);
+      two_sum(v.hi, -s, s2, err2);
+      return quick_two_sum(s2, __fadd_rn(__fsub_rn(v.lo, t), err2));
+    }
+
     // Sum over the CTA of v, where only warps w < nw hold data: their lanes reduce with shuffles, their
     // leaders' sums are added by warp 0.
     __device__ ff cta_sum(ff v, ff* red, int nw) {
@@ -365,7 +399,7 @@ namespace flygpu {
       int const lane = threadIdx.x & 31;
       ff s2 = {0.f, 0.f};
       for (int j = lane; j < m; j += 32) {
-        ff const v = ff_add(ri[j], ff_neg(ff_add(ff_mul(ui, w[j]), ff_mul(wi, u[j]))));
+        ff const v = ff_sub_dot2(ri[j], ui, w[j], wi, u[j]);
         ri[j] = v;
         if (j >= 1) {
           un[j - 1] = v;
@@ -390,10 +424,9 @@ namespace flygpu {
 #pragma unroll
         for (int t = 0; t < 4; ++t) v[t] = ri[j + 32 * t];
 #pragma unroll
-        for (int t = 0; t < 4; ++t)
-          ri[j + 32 * t] = ff_add(v[t], ff_neg(ff_add(ff_mul(ui, w[j + 32 * t]), ff_mul(wi, u[j + 32 * t]))));
+        for (int t = 0; t < 4; ++t) ri[j + 32 * t] = ff_sub_dot2(v[t], ui, w[j + 32 * t], wi, u[j + 32 * t]);
       }
-      for (; j < m; j += 32) ri[j] = ff_add(ri[j], ff_neg(ff_add(ff_mul(ui, w[j]), ff_mul(wi, u[j]))));
+      for (; j < m; j += 32) ri[j] = ff_sub_dot2(ri[j], ui, w[j], wi, u[j]);
     }
 
     // One warp of the owner copies step s's u (m values) and tau from its shared memory into every other
@@ -461,10 +494,11 @@ namespace flygpu {
 #pragma unroll
             for (int t = 0; t < 4; ++t) v[t] = ri[j + 32 * t];
 #pragma unroll
-            for (int t = 0; t < 4; ++t) acc[t] = ff_add(acc[t], ff_mul(v[t], u[j + 32 * t]));
+            for (int t = 0; t < 4; ++t) ff_dot_step(acc[t], v[t], u[j + 32 * t]);
           }
-          for (; j < m; j += 32) acc[0] = ff_add(acc[0], ff_mul(ri[j], u[j]));
-          ff const a = warp_sum_bcast(ff_add(ff_add(acc[0], acc[1]), ff_add(acc[2], acc[3])));
+          for (; j < m; j += 32) ff_dot_step(acc[0], ri[j], u[j]);
+          ff const a =
+            warp_sum_bcast(ff_add(ff_add(ff_norm(acc[0]), ff_norm(acc[1])), ff_add(ff_norm(acc[2]), ff_norm(acc[3]))));
           ff const pi = ff_mul(tau, a);
           if (lane < C) *cl.map_shared_rank(pa + i, lane) = pi;
           sh = ff_add(sh, ff_mul(u[i - b], pi));
