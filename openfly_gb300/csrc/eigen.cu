@@ -2,31 +2,32 @@
 // Hessian::eigenvalues, system/hessian.hpp:86-93, which the reference hands to Eigen's
 // SelfAdjointEigenSolver: Householder tridiagonalisation, then the tridiagonal's eigenvalues).
 //
-// Stage 1, k_tridiag: Householder reduction to tridiagonal form by one thread-block cluster (16 CTAs
-// where the GPU allows it, else 8, 4, ...). CTA c owns the rows i with i mod C == c and keeps them in its
-// shared memory when they fit (ceil(M / C) rows: 66 KB a CTA for M = 342), else in the global matrix.
-// Step k, for the trailing block below row k:
-//   every CTA reads row k (from its owner's shared memory) and forms the same reflector:
-//   alpha = -sign(x0) |x| for x = A[k, k+1:], u = x - alpha e1, tau = 1 / (alpha^2 - alpha x0), so
-//   H = I - tau u u^T maps x to alpha e1;
-//   owned rows: p_i = tau sum_j A[i, j] u_j, and the CTA's share of u^T p;
-//   cluster barrier;
-//   every CTA: K = tau / 2 sum (u^T p), w = p - K u (p read from the owners' shared memory);
-//   owned rows: A[i, j] -= u_i w_j + w_i u_j;
-//   cluster barrier.
-// d_k = A[k, k], e_k = alpha. Every CTA runs the same loop with the same trip count and no early exit, so
-// every barrier is reached by all of them (hardware cluster barriers, not spin loops). On the global path
-// the rows are read with ld.global.cg (L2, not L1) after the barriers' release/acquire.
+// Stage 1: Householder reduction to tridiagonal form by one thread-block cluster. CTA c of C owns the
+// rows i with i mod C == c. Step k, for the trailing block below row k:
+//   the reflector from row k: alpha = -sign(x0) |x| for x = A[k, k+1:], u = x - alpha e1,
+//   tau = 1 / (alpha^2 - alpha x0), so H = I - tau u u^T maps x to alpha e1;
+//   owned rows: p_i = tau sum_j A[i, j] u_j, and their share of u^T p;      cluster barrier;
+//   K = tau / 2 sum (u^T p), w = p - K u;  owned rows: A[i, j] -= u_i w_j + w_i u_j;   cluster barrier.
+// d_k = A[k, k], e_k = alpha. k_tridiag_push, when every CTA's rows fit in its shared memory (8 CTAs
+// for M up to ~460, 16 up to ~640): the producers write into every CTA's shared memory before each
+// barrier (the p_i and the warps' shares before the first; the owner of row k + 1 updates that row
+// first, forms step k + 1's reflector from it and pushes u and tau before the second), so every step
+// starts with its inputs local. k_tridiag<false>, for larger M: the rows stay in the global matrix and
+// each step reads row k, the p values and the shares across the cluster. Every CTA runs the same loop
+// with the same trip count and no early exit, so every barrier is reached by all of them (hardware
+// cluster barriers, not spin loops).
 // GB300 issues binary64 at about 1/64 of the binary32 rate (1.6 lanes a clock per SM) and a dependent
 // binary64 operation takes ~67 cycles, so the O(M^3) work (the rows, u, w, p and every dot product) is
 // float-float arithmetic on the binary32 units (~48 significant bits, far inside the eigenvalues'
-// 1e-10-of-the-spectral-radius tolerance), and so are the per-step scalars. Reductions run on the
-// warps that hold data, and rows are walked in full groups of four plus a one-wide tail.
-// Stage 2, k_bisect: the tridiagonal's eigenvalues by Sturm-sequence multisection, one warp per
-// eigenvalue index j: the 32 lanes count the eigenvalues below 32 points of the current interval (sign
-// changes of the leading principal minors of T - x I, a division-free three-term recurrence), the
-// interval shrinks to the sub-interval holding eigenvalue j, and the loop stops when it is within 4 ulp
-// of its endpoints or of 2 eps |T|. Ascending order comes from j.
+// 1e-10-of-the-spectral-radius tolerance), and so are the per-step scalars. The inner loops keep
+// products as unnormalised pairs and renormalise once per element (the update) or once per row (the
+// dot products).
+// Stage 2, k_tri_prep then k_bisect: the tridiagonal's eigenvalues by Sturm-sequence multisection, one
+// warp per eigenvalue index j: the 32 lanes count the eigenvalues below 32 points of the current
+// interval (sign changes of the leading principal minors of T - x I, a division-free three-term
+// recurrence), and the interval shrinks to the sub-interval holding eigenvalue j: in binary32 while it is
+// wide, then, widened by the binary32 counts' reach, in float-float until it is within 4 ulp of its
+// endpoints or of 2 eps |T|. Ascending order comes from j.
 
 #include <cooperative_groups.h>
 
@@ -249,10 +250,10 @@ namespace flygpu {
 #pragma unroll
             for (int t = 0; t < 4; ++t) v[t] = ld<SM>(ri + j + 32 * t);
 #pragma unroll
-            for (int t = 0; t < 4; ++t) acc[t] = ff_add(acc[t], ff_mul(v[t], u[j + 32 * t]));
+            for (int t = 0; t < 4; ++t) ff_dot_step(acc[t], v[t], u[j + 32 * t]);
           }
-          for (; j < m; j += 32) acc[0] = ff_add(acc[0], ff_mul(ld<SM>(ri + j), u[j]));
-          ff a = ff_add(ff_add(acc[0], acc[1]), ff_add(acc[2], acc[3]));
+          for (; j < m; j += 32) ff_dot_step(acc[0], ld<SM>(ri + j), u[j]);
+          ff a = ff_add(ff_add(ff_norm(acc[0]), ff_norm(acc[1])), ff_add(ff_norm(acc[2]), ff_norm(acc[3])));
           for (int o = 16; o > 0; o >>= 1) a = ff_add(a, ff_shfl_down(a, o));
           if (lane == 0) {
             ff const pi = ff_mul(tau, a);
@@ -292,10 +293,9 @@ namespace flygpu {
 #pragma unroll
             for (int t = 0; t < 4; ++t) v[t] = ld<SM>(ri + j + 32 * t);
 #pragma unroll
-            for (int t = 0; t < 4; ++t)
-              st<SM>(ri + j + 32 * t, ff_add(v[t], ff_neg(ff_add(ff_mul(ui, w[j + 32 * t]), ff_mul(wi, u[j + 32 * t])))));
+            for (int t = 0; t < 4; ++t) st<SM>(ri + j + 32 * t, ff_sub_dot2(v[t], ui, w[j + 32 * t], wi, u[j + 32 * t]));
           }
-          for (; j < m; j += 32) st<SM>(ri + j, ff_add(ld<SM>(ri + j), ff_neg(ff_add(ff_mul(ui, w[j]), ff_mul(wi, u[j])))));
+          for (; j < m; j += 32) st<SM>(ri + j, ff_sub_dot2(ld<SM>(ri + j), ui, w[j], wi, u[j]));
         }
         cl.sync();
       }
@@ -733,9 +733,9 @@ namespace flygpu {
       return ok;
     }
 
-    // Launches the tridiagonalisation of the M x M matrix A (global) on stream s: the largest cluster
-    // (16, 8, ... CTAs) the device can hold, with the rows in shared memory (k_tridiag_push) when they fit,
-    // else in the global matrix. The kernels' shared-memory limits are set to the same constant on every
+    // Launches the tridiagonalisation of the M x M matrix A (global) on stream s: with the rows in shared
+    // memory (k_tridiag_push) on the first cluster of 8, 16, 4, ... CTAs that holds them, else in the
+    // global matrix on the largest cluster the device can hold. The kernels' shared-memory limits are set to the same constant on every
     // call, so concurrent callers agree.
     void tridiag_launch(double* A, int M, double* d, double* e, cudaStream_t s) {
       FLY_CUDA(cudaFuncSetAttribute(k_tridiag_push, cudaFuncAttributeMaxDynamicSharedMemorySize, TRIDIAG_SMEM_MAX));
@@ -743,17 +743,20 @@ namespace flygpu {
       FLY_CUDA(cudaFuncSetAttribute(k_tridiag<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, TRIDIAG_SMEM_MAX));
       FLY_CUDA(cudaFuncSetAttribute(k_tridiag<false>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
       for (int C : {8, 16, 4, 2, 1}) {
-        std::size_t const sp = tridiag_push_smem(M, C), sg = tridiag_smem(M, C, false);
+        std::size_t const sp = tridiag_push_smem(M, C);
+        if (!cluster_fits(k_tridiag_push, C, sp)) continue;
         cudaLaunchAttribute at{};
-        if (cluster_fits(k_tridiag_push, C, sp)) {
-          cudaLaunchConfig_t const cfg = tridiag_config(C, sp, at, s);
-          FLY_CUDA(cudaLaunchKernelEx(&cfg, k_tridiag_push, static_cast<double const*>(A), M, d, e));
-        } else if (cluster_fits(k_tridiag<false>, C, sg)) {
-          cudaLaunchConfig_t const cfg = tridiag_config(C, sg, at, s);
-          FLY_CUDA(cudaLaunchKernelEx(&cfg, k_tridiag<false>, A, M, d, e));
-        } else {
-          continue;
-        }
+        cudaLaunchConfig_t const cfg = tridiag_config(C, sp, at, s);
+        FLY_CUDA(cudaLaunchKernelEx(&cfg, k_tridiag_push, static_cast<double const*>(A), M, d, e));
+        count_launch();
+        return;
+      }
+      for (int C : {16, 8, 4, 2, 1}) {
+        std::size_t const sg = tridiag_smem(M, C, false);
+        if (!cluster_fits(k_tridiag<false>, C, sg)) continue;
+        cudaLaunchAttribute at{};
+        cudaLaunchConfig_t const cfg = tridiag_config(C, sg, at, s);
+        FLY_CUDA(cudaLaunchKernelEx(&cfg, k_tridiag<false>, A, M, d, e));
         count_launch();
         return;
       }

@@ -100,6 +100,24 @@ def test_mass_weighted_eigenvalues_vs_oracle(gpu, oracle, geam, odata, name, s, 
         assert int((np.abs(ev) <= tol).sum()) >= 3 * n_frozen
 
 
+@pytest.mark.parametrize("radius,lo,hi", [(8.0, 460, 640), (8.9, 650, 900)], ids=["cluster16", "global_rows"])
+def test_large_active_block_eigenvalues_vs_oracle(gpu, oracle, geam, odata, radius, lo, hi):
+    # active blocks past the 8-CTA shared-memory size (M > ~460 coordinates: a 16-CTA cluster) and past
+    # the 16-CTA one (M > ~640: rows in the global matrix)
+    rng = np.random.default_rng(5)
+    pos = W.bcc_sites(8, 8, 8, W.A_FE) + rng.normal(0, 0.04, (1024, 3))
+    ext = np.full(3, 8 * W.A_FE)
+    frozen = (np.linalg.norm(pos - ext / 2, axis=1) > radius).astype(np.uint8)
+    M = 3 * int((frozen == 0).sum())
+    assert lo < M < hi, M
+    s = W.System(pos, np.zeros(1024, np.uint32), frozen, ext, np.ones(3, np.int32), {})
+    g, o = _pair(gpu, oracle, odata, s, odata.r_cut)
+    ev, w = geam.hessian_eigenvalues(s.types, s.frozen, g, weighted=True)
+    ref = oracle.hessian_eigenvalues(oracle.eam_hessian(odata, o, s.types, s.frozen, threads=4), _masses(odata, s.types))
+    assert np.all(np.diff(ev) >= 0)
+    assert np.abs(ev - ref).max() <= EIG_TOL * np.abs(ref).max()
+
+
 def test_explicit_masses(gpu, oracle, geam, odata):
     s = W.cluster(np.random.default_rng(8), 8.0, n_h=1).sys
     g, o = _pair(gpu, oracle, odata, s, odata.r_cut)
