@@ -131,7 +131,8 @@ int flygpu_eam_hessian(flygpu_eam* eam, flygpu_list* list, const uint32_t* types
  * built, weighted and diagonalised on the device (the prefactor step of find.cpp:838-871 and
  * Master::calc_minima_hess, find.cpp:1094-1144). masses: one per type (n_types doubles), NULL for the
  * potential file's masses. eig: 3n doubles, ascending. hess (may be NULL): 9 n^2 doubles receiving the
- * mass-weighted matrix. */
+ * mass-weighted matrix. The active atoms' block is diagonalised (at most 9000 coordinates, with a
+ * Gershgorin norm below 2^30; FLYGPU_INVALID_ARG otherwise); each frozen coordinate adds an exact zero. */
 int flygpu_hessian_eigenvalues(flygpu_eam* eam, flygpu_list* list, const uint32_t* types, const uint8_t* frozen,
                                const double* masses, double* eig, double* hess);
 
@@ -320,7 +321,7 @@ int flygpu_minimise(flygpu_eam* eam, const flygpu_lbfgs_options* lbfgs, int prec
  * flygpu_hessian_eigenvalues computes them, with each system's own list at the potential's cut-off.
  * systems: n, pos, types, frozen, extents and periodic of each descriptor are read (the search fields are
  * ignored). The systems run on `workers` host threads (<= 0: 8), each with its own stream and list, so
- * their eigensolves (each one thread-block cluster of up to 16 SMs) overlap on the GPU. eig: the 3 n_k ascending
+ * their eigensolves (each one thread-block cluster of 8 or 16 SMs) overlap on the GPU. eig: the 3 n_k ascending
  * eigenvalues of every system, concatenated in order. masses: per type, NULL for the file's. */
 int flygpu_hessian_eigenvalues_batch(flygpu_eam* eam, const flygpu_search_desc* systems, int n_systems,
                                      const double* masses, int workers, double* eig);
