@@ -505,10 +505,17 @@ namespace flygpu {
         }
         if (lane < C) cl.map_shared_rank(shs, lane)[c * TW + warp] = sh;
         cl.sync();
-        // K = tau / 2 sum of every warp's share: the same order in every warp of every CTA
-        ff t = {0.f, 0.f};
-        for (int q = lane; q < C * TW; q += 32) t = ff_add(t, shs[q]);
-        ff const K = ff_mul(ff_mul(tau, warp_sum_bcast(t)), ff{0.5f, 0.f});
+        // K = tau / 2 sum of every warp's share: the same order in every warp of every CTA (each lane
+        // adds its shares pairwise: at most 8, for 16 CTAs of 16 warps; missing ones are zeros)
+        ff t[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) t[q] = lane + 32 * q < C * TW ? shs[lane + 32 * q] : ff{0.f, 0.f};
+        if (C * TW > 128) {
+#pragma unroll
+          for (int q = 0; q < 4; ++q) t[q] = ff_add(t[q], t[q + 4]);
+        }
+        t[0] = ff_add(ff_add(t[0], t[2]), ff_add(t[1], t[3]));
+        ff const K = ff_mul(ff_mul(tau, warp_sum_bcast(t[0])), ff{0.5f, 0.f});
         for (int j = threadIdx.x; j < m; j += TT) w[j] = ff_add(pa[b + j], ff_neg(ff_mul(K, u[j])));
         __syncthreads();
         bool const next = k + 3 < M;  // a step k + 1 follows
@@ -559,7 +566,13 @@ namespace flygpu {
       if (p.hi == 0.f) p = {-0x1p-40f, 0.f};
       int cnt = p.hi < 0.f;
       for (int i = 1; i < M; ++i) {
-        ff pn = ff_add(ff_mul(ff_add(d[i], nx), p), ff_neg(ff_mul(e2[i - 1], pm)));
+        // (d_i - x) p - e_{i-1}^2 pm: both products as unnormalised pairs, one TwoSum of their leading
+        // parts, one renormalisation (the product with pm is off the recurrence's dependent chain)
+        float p1, e1, p2, e2x, s, err;
+        ff_prod(ff_add(d[i], nx), p, p1, e1);
+        ff_prod(e2[i - 1], pm, p2, e2x);
+        two_sum(p1, -p2, s, err);
+        ff pn = quick_two_sum(s, __fadd_rn(__fsub_rn(e1, e2x), err));
         if (pn.hi == 0.f) pn = {-p.hi * 0x1p-40f, 0.f};
         cnt += (pn.hi < 0.f) != (p.hi < 0.f);
         pm = p;
