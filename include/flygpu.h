@@ -83,7 +83,9 @@ void flygpu_list_destroy(flygpu_list* list);
 int flygpu_list_rebuild(flygpu_list* list, const double* pos, int64_t n);
 int flygpu_list_rebuild_device(flygpu_list* list, const double* d_pos, int64_t n);
 /* List::update (neigh/list.hpp:118, src/neigh/list.cpp:37-51): r <- r - delta for real and ghost
- * atoms. delta: 3n doubles. */
+ * atoms. delta: 3n doubles. The call returns once the update is queued on the list's stream; a delta in
+ * pinned (page-locked) host memory is copied asynchronously, so keep it unchanged until the list's next
+ * synchronising call (any EAM call that returns results to the host). */
 int flygpu_list_update(flygpu_list* list, const double* delta);
 int flygpu_list_update_device(flygpu_list* list, const double* d_delta);
 /* List::size (neigh/list.hpp:161) */
@@ -111,7 +113,9 @@ int flygpu_eam_energy(flygpu_eam* eam, flygpu_list* list, const uint32_t* types,
 /* EAM::gradient (potential/EAM/eam.hpp:95, src/potential/EAM/eam.cpp:53-120). grad: 3n doubles. */
 int flygpu_eam_gradient(flygpu_eam* eam, flygpu_list* list, const uint32_t* types, const uint8_t* frozen,
                         int precision, double* grad);
-/* Both in one density pass + one force pass (energy may be NULL). */
+/* Both in one density pass + one force pass (energy may be NULL). A grad buffer in pinned host memory
+ * receives the force pass's stores directly (the transfer overlaps the pass); other memory receives a
+ * copy after it. Either way the call returns with the results in place. */
 int flygpu_eam_energy_gradient(flygpu_eam* eam, flygpu_list* list, const uint32_t* types,
                                const uint8_t* frozen, int precision, double* energy, double* grad);
 /* Device-pointer form of the above: d_types / d_frozen may be NULL (reuse), d_energy may be NULL. */
