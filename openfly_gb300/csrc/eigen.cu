@@ -12,7 +12,7 @@
 // for M up to ~460, 16 up to ~640): the producers write into every CTA's shared memory before each
 // barrier (the p_i and the warps' shares before the first; the owner of row k + 1 updates that row
 // first, forms step k + 1's reflector from it and pushes u and tau before the second), so every step
-// starts with its inputs local. k_tridiag<false>, for larger M: the rows stay in the global matrix and
+// starts with its inputs local. k_tridiag_global, for larger M: the rows stay in the global matrix and
 // each step reads row k, the p values and the shares across the cluster. Every CTA runs the same loop
 // with the same trip count and no early exit, so every barrier is reached by all of them (hardware
 // cluster barriers, not spin loops).
@@ -137,76 +137,45 @@ namespace flygpu {
       return s;
     }
 
-    // The rows of the matrix a CTA owns: in its shared memory (SM) or in the global matrix, as float-float.
-    template <bool SM>
-    struct Rows {
-      ff* base;  // SM: the CTA's rows, local row r at base + r M; else the global matrix
-      int M, C;
-      __device__ ff* own(int i) const {
-        return SM ? base + static_cast<std::int64_t>(i / C) * M : base + static_cast<std::int64_t>(i) * M;
-      }
-    };
-
-    template <bool SM>
+    // A float-float element of the global matrix, read and written through L2 (ld.global.cg / st.global.cg:
+    // other CTAs of the cluster write these rows between the barriers).
     __device__ inline ff ld(ff const* p) {
-      if constexpr (SM) {
-        return *p;
-      } else {
-        float2 const v = __ldcg(reinterpret_cast<float2 const*>(p));
-        return {v.x, v.y};
-      }
+      float2 const v = __ldcg(reinterpret_cast<float2 const*>(p));
+      return {v.x, v.y};
     }
-    template <bool SM>
-    __device__ inline void st(ff* p, ff v) {
-      if constexpr (SM) {
-        *p = v;
-      } else {
-        __stcg(reinterpret_cast<float2*>(p), make_float2(v.hi, v.lo));
-      }
-    }
+    __device__ inline void st(ff* p, ff v) { __stcg(reinterpret_cast<float2*>(p), make_float2(v.hi, v.lo)); }
 
-    // Householder tridiagonalisation of the M x M symmetric A (binary64, full storage; overwritten on
-    // the global path, where it is first converted in place to float-float). d: M, e: M (e[M-1]
-    // unused). Launched as one cluster of C CTAs; CTA c owns the rows i with i mod C == c. With SM every
-    // CTA keeps its rows in shared memory (ceil(M / C) rows). Row k, the p values and the CTAs' shares
-    // of u^T p are read across the cluster through distributed shared memory. The matrix, u, w, p and
-    // every dot product are float-float, and so are the per-step scalars |x|, alpha and tau (binary32
-    // seeds refined by one float-float Newton step).
-    template <bool SM>
-    __global__ void __launch_bounds__(TT) k_tridiag(double* __restrict__ A, int M, double* __restrict__ d,
-                                                   double* __restrict__ e) {
+    // Householder tridiagonalisation of the M x M symmetric A (binary64, full storage) with the rows in
+    // the global matrix: A is first converted in place to float-float and then overwritten. d: M, e: M
+    // (e[M-1] unused). Launched as one cluster of C CTAs; CTA c owns the rows i with i mod C == c. Row k
+    // is read from the matrix, the p values and the CTAs' shares of u^T p across the cluster through
+    // distributed shared memory. The matrix, u, w, p and every dot product are float-float, and so are
+    // the per-step scalars |x|, alpha and tau (binary32 seeds refined by one float-float Newton step).
+    __global__ void __launch_bounds__(TT) k_tridiag_global(double* __restrict__ A, int M, double* __restrict__ d,
+                                                          double* __restrict__ e) {
       cg::cluster_group cl = cg::this_cluster();
       int const C = static_cast<int>(cl.num_blocks());
       int const c = static_cast<int>(cl.block_rank());
-      int const R = (M + C - 1) / C;
       extern __shared__ ff sm[];
-      ff* rows = sm;                                              // SM: R x M
-      ff* u = sm + (SM ? static_cast<std::int64_t>(R) * M : 0);  // M
+      ff* u = sm;                                                 // M
       ff* w = u + M;                                              // M
       ff* pl = w + M;                                             // M: p_i of the owned rows, at index i
       ff* share = pl + M;                                         // 1
       ff* red = share + 1;                                        // TW + 1
       int const lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-      ff* const Aff = reinterpret_cast<ff*>(A);  // the global path's rows, converted in place
-      Rows<SM> const own{SM ? rows : Aff, M, C};
+      ff* const Aff = reinterpret_cast<ff*>(A);  // the rows, converted in place
       for (int r = warp; r * C + c < M; r += TW)
         for (int j = lane; j < M; j += 32) {
           std::int64_t const g = static_cast<std::int64_t>(r * C + c) * M + j;
-          ff const v = ff_of(__ldcg(A + g));
-          if (SM) {
-            rows[static_cast<std::int64_t>(r) * M + j] = v;
-          } else {
-            st<false>(Aff + g, v);
-          }
+          st(Aff + g, ff_of(__ldcg(A + g)));
         }
       cl.sync();
       for (int k = 0; k + 2 < M; ++k) {
         int const b = k + 1, m = M - b;
-        ff const* rk = SM ? cl.map_shared_rank(rows, k % C) + static_cast<std::int64_t>(k / C) * M
-                          : Aff + static_cast<std::int64_t>(k) * M;
+        ff const* rk = Aff + static_cast<std::int64_t>(k) * M;
         ff s2 = {0.f, 0.f};
         for (int j = threadIdx.x; j < m; j += TT) {
-          ff const x = ld<SM>(rk + b + j);
+          ff const x = ld(rk + b + j);
           u[j] = x;
           s2 = ff_add(s2, ff_mul(x, x));
         }
@@ -232,7 +201,7 @@ namespace flygpu {
         __syncthreads();
         if (threadIdx.x == 0) u[0] = reflect ? ff_add(x0, ff_neg(alpha)) : ff{0.f, 0.f};
         if (c == 0 && threadIdx.x == 0) {
-          d[k] = ff_dbl(ld<SM>(rk + k));
+          d[k] = ff_dbl(ld(rk + k));
           e[k] = ff_dbl(reflect ? alpha : x0);
         }
         __syncthreads();
@@ -242,17 +211,17 @@ namespace flygpu {
         for (int r = warp; r * C + c < M; r += TW) {
           int const i = r * C + c;
           if (i < b) continue;
-          ff const* ri = own.own(i) + b;
+          ff const* ri = (Aff + static_cast<std::int64_t>(i) * M) + b;
           ff acc[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
           int j = lane;
           for (; j + 96 < m; j += 128) {
             ff v[4];
 #pragma unroll
-            for (int t = 0; t < 4; ++t) v[t] = ld<SM>(ri + j + 32 * t);
+            for (int t = 0; t < 4; ++t) v[t] = ld(ri + j + 32 * t);
 #pragma unroll
             for (int t = 0; t < 4; ++t) ff_dot_step(acc[t], v[t], u[j + 32 * t]);
           }
-          for (; j < m; j += 32) ff_dot_step(acc[0], ld<SM>(ri + j), u[j]);
+          for (; j < m; j += 32) ff_dot_step(acc[0], ld(ri + j), u[j]);
           ff a = ff_add(ff_add(ff_norm(acc[0]), ff_norm(acc[1])), ff_add(ff_norm(acc[2]), ff_norm(acc[3])));
           for (int o = 16; o > 0; o >>= 1) a = ff_add(a, ff_shfl_down(a, o));
           if (lane == 0) {
@@ -284,25 +253,24 @@ namespace flygpu {
         for (int r = warp; r * C + c < M; r += TW) {
           int const i = r * C + c;
           if (i < b) continue;
-          ff* ri = own.own(i) + b;
+          ff* ri = (Aff + static_cast<std::int64_t>(i) * M) + b;
           ff const ui = u[i - b], wi = w[i - b];
           // A_ij - (u_i w_j + w_i u_j)
           int j = lane;
           for (; j + 96 < m; j += 128) {
             ff v[4];
 #pragma unroll
-            for (int t = 0; t < 4; ++t) v[t] = ld<SM>(ri + j + 32 * t);
+            for (int t = 0; t < 4; ++t) v[t] = ld(ri + j + 32 * t);
 #pragma unroll
-            for (int t = 0; t < 4; ++t) st<SM>(ri + j + 32 * t, ff_sub_dot2(v[t], ui, w[j + 32 * t], wi, u[j + 32 * t]));
+            for (int t = 0; t < 4; ++t) st(ri + j + 32 * t, ff_sub_dot2(v[t], ui, w[j + 32 * t], wi, u[j + 32 * t]));
           }
-          for (; j < m; j += 32) st<SM>(ri + j, ff_sub_dot2(ld<SM>(ri + j), ui, w[j], wi, u[j]));
+          for (; j < m; j += 32) st(ri + j, ff_sub_dot2(ld(ri + j), ui, w[j], wi, u[j]));
         }
         cl.sync();
       }
       if (c == 0 && threadIdx.x == 0) {
         auto at = [&](int i, int j) {
-          return ff_dbl(SM ? cl.map_shared_rank(rows, i % C)[static_cast<std::int64_t>(i / C) * M + j]
-                           : ld<false>(Aff + static_cast<std::int64_t>(i) * M + j));
+          return ff_dbl(ld(Aff + static_cast<std::int64_t>(i) * M + j));
         };
         if (M >= 2) {
           d[M - 2] = at(M - 2, M - 2);
@@ -714,9 +682,8 @@ namespace flygpu {
       out[t] = a >= b ? H[a * N + b] : H[b * N + a];
     }
 
-    std::size_t tridiag_smem(int M, int C, bool sm) {
-      std::size_t const R = sm ? static_cast<std::size_t>((M + C - 1) / C) : 0;
-      return (R * static_cast<std::size_t>(M) + 3 * static_cast<std::size_t>(M) + 1 + TW + 1) * sizeof(double);  // 8-byte elements
+    std::size_t tridiag_global_smem(int M) {  // u, w, p (M each), the share and TW + 1 reduction slots
+      return (3 * static_cast<std::size_t>(M) + 1 + TW + 1) * sizeof(double);  // 8-byte elements
     }
 
     cudaLaunchConfig_t tridiag_config(int C, std::size_t smem, cudaLaunchAttribute& at, cudaStream_t s) {
@@ -753,8 +720,8 @@ namespace flygpu {
     void tridiag_launch(double* A, int M, double* d, double* e, cudaStream_t s) {
       FLY_CUDA(cudaFuncSetAttribute(k_tridiag_push, cudaFuncAttributeMaxDynamicSharedMemorySize, TRIDIAG_SMEM_MAX));
       FLY_CUDA(cudaFuncSetAttribute(k_tridiag_push, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
-      FLY_CUDA(cudaFuncSetAttribute(k_tridiag<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, TRIDIAG_SMEM_MAX));
-      FLY_CUDA(cudaFuncSetAttribute(k_tridiag<false>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+      FLY_CUDA(cudaFuncSetAttribute(k_tridiag_global, cudaFuncAttributeMaxDynamicSharedMemorySize, TRIDIAG_SMEM_MAX));
+      FLY_CUDA(cudaFuncSetAttribute(k_tridiag_global, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
       for (int C : {8, 16, 4, 2, 1}) {
         std::size_t const sp = tridiag_push_smem(M, C);
         if (!cluster_fits(k_tridiag_push, C, sp)) continue;
@@ -765,11 +732,11 @@ namespace flygpu {
         return;
       }
       for (int C : {16, 8, 4, 2, 1}) {
-        std::size_t const sg = tridiag_smem(M, C, false);
-        if (!cluster_fits(k_tridiag<false>, C, sg)) continue;
+        std::size_t const sg = tridiag_global_smem(M);
+        if (!cluster_fits(k_tridiag_global, C, sg)) continue;
         cudaLaunchAttribute at{};
         cudaLaunchConfig_t const cfg = tridiag_config(C, sg, at, s);
-        FLY_CUDA(cudaLaunchKernelEx(&cfg, k_tridiag<false>, A, M, d, e));
+        FLY_CUDA(cudaLaunchKernelEx(&cfg, k_tridiag_global, A, M, d, e));
         count_launch();
         return;
       }
