@@ -1,18 +1,19 @@
 // hessian.cu -- EAM Hessian, mass weighting and eigenvalues (compiled with -fmad=false).
 //
-// Restates EAM::hessian (src/potential/EAM/eam.cpp:122-233) on the device. Pass 1, one thread per atom
-// b (active and frozen): rho_b = sum_a phi(t_a, t_b)(r) and mu_b = -sum_a phi'(t_a, t_b)(r) dr / r
-// (A.13), with F'(rho_b) and F''(rho_b). Pass 2, one warp (CTA) per active atom z, writes only column block z
-// of the dense 3n x 3n matrix (row-major; the rows of atom a are 3a..3a+2):
+// Restates EAM::hessian (src/potential/EAM/eam.cpp:122-233) on the device. Pass 1, one warp per atom b
+// (active and frozen): rho_b = sum_a phi(t_a, t_b)(r) and mu_b = -sum_a phi'(t_a, t_b)(r) dr / r
+// (A.13), with F'(rho_b) and F''(rho_b); it also keeps every pair's distance, phi' and destination key
+// for pass 2. Pass 2, one CTA per active atom z, writes only column block z of the dense 3n x 3n matrix
+// (row-major; the rows of atom a are 3a..3a+2):
 //   H(z,z) = F''_z mu_z mu_z^T + sum_a [A 1 - ABFpp dr dr^T]                           (A.15, A.14)
 //   H(a,z) += -BArr dr dr^T - A 1 + ur dr mu_z^T - ru mu_a dr^T       for active a > z
 //   H(g,z) -= F''_a phi'(t_z,t_a)(r) phi'(t_g,t_a)(r_ag) / (r r_ag) dr_ag dr^T
 //             for every neighbour g of a that is active with g > z, or a periodic image of z itself.
-// Neighbours come from the list in the reference's visiting order, every coefficient is formed in the
-// reference's operation order, and every element receives its contributions in the reference's order:
-// lane 0 adds the (z,z) and (a,z) terms of neighbour a, then the warp's lanes split a's neighbours g,
-// so each (g,z) block takes the contributions of successive a in the order of the serial loop (equal g
-// within one group of 32 are applied in list order, one occurrence per round). The result is the
+// Neighbours come from the list in the reference's visiting order and every coefficient is formed in
+// the reference's operation order. The serial loop's contributions (for each a: the (z,z) term, the
+// (a,z) term, then the (g,z) terms) are queued in that order; each destination block's contributions
+// are applied in queue order (by occurrence levels, the (z,z) block as its own chain). So every
+// element receives the reference's contributions in the reference's order, and the result is the
 // matrix the reference's loops build, bit for bit.
 //
 // Hessian::mass_weight (system/hessian.hpp:136-143) scales block (j, i) by 1/sqrt(m_i m_j), and
