@@ -77,6 +77,25 @@ namespace flygpu {
     launch(k_unfinished, 1, 1024, 0, s, S, order, n, order_out, n_out);
   }
 
+  namespace {
+    __global__ void k_image_scatter(char* __restrict__ block, char const* __restrict__ src,
+                                    ImageChunk const* __restrict__ ch, int n) {
+      int const w = static_cast<int>((static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5);
+      int const lane = threadIdx.x & 31;
+      if (w >= n) return;
+      ImageChunk const c = ch[w];
+      long long const words = c.bytes / 8;
+      auto* d8 = reinterpret_cast<unsigned long long*>(block + c.dst);
+      auto const* s8 = reinterpret_cast<unsigned long long const*>(src + c.src);
+      for (long long i = lane; i < words; i += 32) d8[i] = s8[i];
+      for (long long i = words * 8 + lane; i < c.bytes; i += 32) block[c.dst + i] = src[c.src + i];
+    }
+  }  // namespace
+
+  void search_image_scatter(char* block, char const* d_src, ImageChunk const* d_chunks, int n, cudaStream_t s) {
+    if (n > 0) launch(k_image_scatter, static_cast<unsigned>((n + 7) / 8), 256, 0, s, block, d_src, d_chunks, n);
+  }
+
   SearchLayout search_layout(int n, int na, int n_vec_doubles, int n_hist_doubles) {
     auto up = [](std::size_t b) { return (b + 255) / 256 * 256; };
     SearchLayout l{};

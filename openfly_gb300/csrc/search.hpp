@@ -136,14 +136,26 @@ namespace flygpu {
   // call before any graph capture).
   void search_init_kernels();
   SearchLayout search_layout(int n, int na, int n_vec_doubles, int n_hist_doubles);
+  // A region of a search image written on the host: `bytes` bytes from `src` of a compact host buffer to
+  // byte `dst` of the device block. The rest of a block starts as zeros.
+  struct ImageChunk {
+    long long dst, src, bytes;
+  };
+  // Copies n chunks from d_src into the (zeroed) block on stream s, one warp per chunk; dst and src are
+  // 8-byte aligned.
+  void search_image_scatter(char* block, char const* d_src, ImageChunk const* d_chunks, int n, cudaStream_t s);
   void search_bind(SearchDev& S, char* base, SearchLayout const& l);
   // The items of order[0..n) whose search has not finished, in the same order, into order_out, and
   // their count into *n_out (device memory). One CTA.
   void search_unfinished(SearchDev const* S, int const* order, int n, int* order_out, int* n_out, cudaStream_t s);
 
-  // search_host.cpp: fill one search's state and initial arrays (image at byte `at` of img).
+  // search_host.cpp: fill one search's state and initial arrays (image at byte `at` of img; a grown img
+  // is zero-filled, a reused one keeps its old bytes outside the regions search_written writes).
   SearchLayout search_prepare(SearchOpts const& o, int n_types, flygpu_search_desc const& d, SearchDev& S,
                               std::vector<int>& mob, std::vector<char>& img, std::size_t at);
+  // The (offset, bytes) regions of a search image that search_prepare writes; every other byte of the
+  // image is zero.
+  std::vector<std::pair<std::size_t, std::size_t>> search_written(SearchLayout const& l, SearchDev const& S);
   SearchOpts make_opts(flygpu_dimer_options const& d, flygpu_lbfgs_options const& l, double r_cut);
 
 }  // namespace flygpu

@@ -279,11 +279,28 @@ namespace flygpu {
     return l;
   }
 
+  std::vector<std::pair<std::size_t, std::size_t>> search_written(SearchLayout const& l, SearchDev const& S) {
+    std::size_t const n = static_cast<std::size_t>(S.n), na = static_cast<std::size_t>(S.na), M = 3 * na;
+    std::vector<std::pair<std::size_t, std::size_t>> r;
+    r.emplace_back(l.xl, sizeof(D4) * n);
+    r.emplace_back(l.vec + sizeof(double) * V_X * M, sizeof(double) * M);
+    if (S.mode == FLYGPU_SEARCH_DIMER) r.emplace_back(l.vec + sizeof(double) * V_AX * M, sizeof(double) * M);
+    r.emplace_back(l.vec + sizeof(double) * V_INMIN * M, sizeof(double) * M);
+    if (S.n_hist > 0) r.emplace_back(l.hist, sizeof(double) * static_cast<std::size_t>(S.n_hist) * (M + 2));
+    r.emplace_back(l.aatom, sizeof(int) * na);
+    r.emplace_back(l.type, n);
+    r.emplace_back(l.mob, n);
+    return r;
+  }
+
   void batch_build(flygpu_batch* B, flygpu_search_desc const* descs, int n_search) {
     if (n_search <= 0) fail(FLYGPU_INVALID_ARG, "empty batch");
     B->n_search = n_search;
     B->h_S.resize(static_cast<std::size_t>(n_search));
-    std::vector<char> img;
+    // Each search is prepared in one reused scratch image; only the regions it writes go to the device
+    // (most of a search's block, its neighbour columns and work vectors, starts as zeros).
+    std::vector<char> scratch, compact;
+    std::vector<ImageChunk> chunks;
     std::vector<SearchLayout> lay(static_cast<std::size_t>(n_search));
     std::vector<std::size_t> at(static_cast<std::size_t>(n_search));
     std::vector<std::int64_t> h_act3;
@@ -294,7 +311,12 @@ namespace flygpu {
       flygpu_search_desc const& d = descs[s];
       SearchDev& S = B->h_S[static_cast<std::size_t>(s)];
       at[static_cast<std::size_t>(s)] = off;
-      lay[static_cast<std::size_t>(s)] = search_prepare(B->o, B->eam->n_types, d, S, mob, img, off);
+      lay[static_cast<std::size_t>(s)] = search_prepare(B->o, B->eam->n_types, d, S, mob, scratch, 0);
+      for (auto const& [o, b] : search_written(lay[static_cast<std::size_t>(s)], S)) {
+        compact.resize((compact.size() + 15) / 16 * 16);  // 8-byte aligned sources for the scatter
+        chunks.push_back({static_cast<long long>(off + o), static_cast<long long>(compact.size()), static_cast<long long>(b)});
+        compact.insert(compact.end(), scratch.data() + o, scratch.data() + o + b);
+      }
       off += lay[static_cast<std::size_t>(s)].total;
       int const n = S.n, na = S.na;
       B->n_atoms.push_back(n);
@@ -332,7 +354,14 @@ namespace flygpu {
     upload(B->S, B->h_S, st);
     upload(B->order_d, B->order, st);
     upload(B->act3_d, h_act3, st);
-    FLY_CUDA(cudaMemcpyAsync(B->block_init.p, img.data(), off, cudaMemcpyHostToDevice, st));
+    DevBuf<char> d_compact;
+    DevBuf<ImageChunk> d_chunks;
+    d_compact.reserve(std::max<std::size_t>(compact.size(), 1));
+    d_chunks.reserve(std::max<std::size_t>(chunks.size(), 1));
+    FLY_CUDA(cudaMemsetAsync(B->block_init.p, 0, off, st));
+    FLY_CUDA(cudaMemcpyAsync(d_compact.p, compact.data(), compact.size(), cudaMemcpyHostToDevice, st));
+    FLY_CUDA(cudaMemcpyAsync(d_chunks.p, chunks.data(), sizeof(ImageChunk) * chunks.size(), cudaMemcpyHostToDevice, st));
+    search_image_scatter(B->block_init.p, d_compact.p, d_chunks.p, static_cast<int>(chunks.size()), st);
     FLY_CUDA(cudaMemcpyAsync(B->block.p, B->block_init.p, off, cudaMemcpyDeviceToDevice, st));
     B->out_x.reserve(static_cast<std::size_t>(3 * act));
     B->out_ax.reserve(static_cast<std::size_t>(3 * act));
