@@ -68,6 +68,49 @@ class SearchDesc(C.Structure):
     ]
 
 
+def desc_array(searches: list, keep: list):
+    """The SearchDesc array of many searches, filled column by column (one numpy assignment per field
+    instead of one ctypes assignment per field and search); the descriptors point into the searches' own
+    arrays, or into converted copies kept alive by ``keep``. The same contents as
+    ``(SearchDesc * n)(*[s.desc(keep) for s in searches])``."""
+    n = len(searches)
+    out = (SearchDesc * max(1, n))()
+    if n == 0:
+        return out
+    f = {name: getattr(SearchDesc, name).offset for name, _ in SearchDesc._fields_}
+    names = ["n", "pos", "axis", "types", "frozen", "extents", "periodic", "mode", "n_hist", "hist", "in_min",
+             "theta_tol"]
+    dt = np.dtype({"names": names,
+                   "formats": [np.int64, np.uint64, np.uint64, np.uint64, np.uint64, (np.float64, 3), (np.int32, 3),
+                               np.int32, np.int32, np.uint64, np.uint64, np.float64],
+                   "offsets": [f[k] for k in names], "itemsize": C.sizeof(SearchDesc)})
+    rec = np.frombuffer(out, dtype=dt, count=n)
+
+    def col(arrays):
+        keep.extend(arrays)
+        return np.fromiter((0 if a is None else a.ctypes.data for a in arrays), dtype=np.uint64, count=n)
+
+    pos = [np.ascontiguousarray(x.pos, dtype=np.float64) for x in searches]
+    rec["n"] = np.fromiter((p.size // 3 for p in pos), dtype=np.int64, count=n)
+    rec["pos"] = col(pos)
+    rec["axis"] = col([None if x.axis is None else np.ascontiguousarray(x.axis, dtype=np.float64) for x in searches])
+    rec["types"] = col([np.ascontiguousarray(x.types, dtype=np.uint32) for x in searches])
+    rec["frozen"] = col([np.ascontiguousarray(x.frozen, dtype=np.uint8) for x in searches])
+    rec["extents"] = np.array([np.asarray(x.extents, dtype=np.float64).reshape(3) for x in searches])
+    rec["periodic"] = np.array([np.asarray(x.periodic).reshape(3) for x in searches]).astype(np.int32)
+    rec["mode"] = np.fromiter((x.mode for x in searches), dtype=np.int32, count=n)
+    rec["theta_tol"] = np.fromiter((x.theta_tol for x in searches), dtype=np.float64, count=n)
+    rec["n_hist"] = 0
+    rec["hist"] = 0
+    rec["in_min"] = 0
+    for k, x in enumerate(searches):  # the rare per-search extras
+        if x.hist or x.in_min is not None:
+            d = x.desc(keep)
+            rec["n_hist"][k], rec["hist"][k] = d.n_hist, d.hist or 0
+            rec["in_min"][k] = d.in_min or 0
+    return out
+
+
 class SearchResult(C.Structure):
     _fields_ = [
         ("exit_code", C.c_int), ("status", C.c_int), ("steps", C.c_int), ("pad_", C.c_int),
@@ -176,7 +219,7 @@ class Batch:
         _setup()
         self.searches = searches
         keep: list = []
-        descs = (SearchDesc * len(searches))(*[s.desc(keep) for s in searches])
+        descs = desc_array(searches, keep)
         h = C.c_void_p()
         self.dimer = dimer or DimerOptions.defaults()
         self.lbfgs = lbfgs or LBFGSOptions.defaults()
@@ -283,9 +326,7 @@ class Server:
     def submit_many(self, searches: list[Search]) -> list[int]:
         """flygpu_server_submit_many: all of them or none; returns their ids in order."""
         keep: list = []
-        descs = (SearchDesc * max(1, len(searches)))()
-        for k, x in enumerate(searches):
-            descs[k] = x.desc(keep)
+        descs = desc_array(searches, keep)
         ids = np.zeros(max(1, len(searches)), dtype=np.uint64)
         check(lib().flygpu_server_submit_many(self.h, descs, len(searches), ids.ctypes.data), "Server.submit_many")
         out = [int(i) for i in ids[: len(searches)]]
@@ -559,9 +600,7 @@ def hessian_eigenvalues_batch(eam: EAM, systems: list, masses=None, workers: int
     used); masses per type (None: the potential file's)."""
     _setup()
     keep: list = []
-    descs = (SearchDesc * max(1, len(systems)))()
-    for k, s in enumerate(systems):
-        descs[k] = s.desc(keep)
+    descs = desc_array(systems, keep)
     sizes = [3 * s.n for s in systems]
     eig = np.zeros(max(1, sum(sizes)), dtype=np.float64)
     m = None if masses is None else np.ascontiguousarray(masses, dtype=np.float64)
