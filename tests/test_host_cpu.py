@@ -113,3 +113,38 @@ def test_bench_replica_value_and_traffic_table():
     t = bench.traffic_from_profile("k_force32", 1_000_000)
     assert t is not None and 200e6 < t < 400e6
     assert bench.traffic_from_profile("no_such_kernel", 10) is None
+
+
+def test_desc_array_equals_per_search_descriptors():
+    # the column-wise SearchDesc builder of batches, server submissions and Hessian batches gives the
+    # per-search desc() contents, pointed-to bytes included (dimer and minimise modes, a saddle history,
+    # an in_min, a binary32 position array that needs converting)
+    import ctypes as C
+
+    from openfly_gb300 import search as S
+
+    cl = W.search_clusters(n=24, seed=3)
+    reqs = [S.from_cluster(c) for c in cl]
+    reqs[3].hist = [reqs[3].pos + 0.1, reqs[3].pos - 0.2]
+    reqs[3].in_min = reqs[3].pos + 0.05
+    reqs[3].theta_tol = 0.3
+    reqs[5] = S.from_cluster(cl[5], mode=S.MINIMISE)
+    reqs[7].pos = reqs[7].pos.astype(np.float32)
+    k1, k2 = [], []
+    a = (S.SearchDesc * len(reqs))(*[s.desc(k1) for s in reqs])
+    b = S.desc_array(reqs, k2)
+
+    def deref(d, field, cnt, ctype):
+        p = getattr(d, field)
+        return None if not p else bytes((ctype * cnt).from_address(p))
+
+    for x, y in zip(a, b):
+        n = x.n
+        for fld in ("n", "mode", "n_hist", "theta_tol"):
+            assert getattr(x, fld) == getattr(y, fld)
+        assert list(x.extents) == list(y.extents) and list(x.periodic) == list(y.periodic)
+        for fld, cnt, ct in (("pos", 3 * n, C.c_double), ("axis", 3 * n, C.c_double), ("types", n, C.c_uint32),
+                             ("frozen", n, C.c_uint8), ("in_min", 3 * n, C.c_double),
+                             ("hist", 3 * n * max(1, x.n_hist), C.c_double)):
+            assert deref(x, fld, cnt, ct) == deref(y, fld, cnt, ct), fld
+    assert len(S.desc_array([], [])) == 1
