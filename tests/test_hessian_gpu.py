@@ -100,6 +100,22 @@ def test_mass_weighted_eigenvalues_vs_oracle(gpu, oracle, geam, odata, name, s, 
         assert int((np.abs(ev) <= tol).sum()) >= 3 * n_frozen
 
 
+def test_hessian_more_than_128_neighbours_vs_oracle(gpu, oracle, geam, odata):
+    # a bcc lattice compressed to 0.75 of its constant: some atoms have more than 128 neighbours within
+    # the cut-off, so the column pass takes their coefficients in more than one chunk
+    rng = np.random.default_rng(1)
+    a = 0.75 * W.A_FE
+    pos = W.bcc_sites(5, 5, 5, a) + rng.normal(0, 0.02, (250, 3))
+    frozen = np.zeros(250, np.uint8)
+    frozen[:200] = 1
+    s = W.System(pos, np.zeros(250, np.uint32), frozen, np.full(3, 5 * a), np.ones(3, np.int32), {})
+    g, o = _pair(gpu, oracle, odata, s, odata.r_cut)
+    assert int(o.neighbours(odata.r_cut)[0].max()) > 128
+    h = geam.hessian(s.types, s.frozen, g)
+    ref = oracle.eam_hessian(odata, o, s.types, s.frozen, threads=4)
+    assert np.array_equal(h, ref), np.abs(h - ref).max()
+
+
 @pytest.mark.parametrize("radius,lo,hi", [(8.0, 460, 640), (8.9, 650, 900)], ids=["cluster16", "global_rows"])
 def test_large_active_block_eigenvalues_vs_oracle(gpu, oracle, geam, odata, radius, lo, hi):
     # active blocks past the 8-CTA shared-memory size (M > ~460 coordinates: a 16-CTA cluster) and past
