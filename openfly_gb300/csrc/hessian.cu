@@ -148,8 +148,9 @@ namespace flygpu {
     // Pass 2 shape: threads per column CTA, flat slots each thread enumerates per window, the items a
     // window can queue, the neighbours a of z whose coefficients one chunk holds, and the slots of the
     // window's destination table.
-    constexpr int COL_T = 128;
-    constexpr int COL_SLOTS = 8;
+    constexpr int COL_T = 256;
+    constexpr int COL_SLOTS = 4;
+    constexpr int COL_WORK = COL_T - 32;  // threads of warps 1.. (values) and 0.. (levels): all but one warp
     constexpr int COL_W = COL_T * COL_SLOTS;
     constexpr int COL_KC = COL_T;
     constexpr int COL_HASH = 2 * COL_W;
@@ -202,8 +203,8 @@ namespace flygpu {
       return off + x - v;
     }
 
-    // Barrier of warps 0-2 (96 threads) alone; warp 3 meanwhile runs the (z,z) chain.
-    __device__ inline void bar_levels() { asm volatile("bar.sync 1, 96;" ::: "memory"); }
+    // Barrier of every warp but the last (COL_WORK threads); the last warp meanwhile runs the (z,z) chain.
+    __device__ inline void bar_levels() { asm volatile("bar.sync 1, %0;" ::"n"(COL_WORK) : "memory"); }
 
     // Pass 2: column block z, one CTA per active atom (cols lists them). The reference's serial loop over
     // z's neighbours a adds, for each a in list order, the (z,z) term, the (a,z) term, then one (g,z) term
@@ -211,10 +212,10 @@ namespace flygpu {
     // that sequence of items as flat slots, compacts the items that apply into a queue (order kept), and
     // forms their values densely. Each queued item then gets its occurrence number: how often its
     // destination block occurs earlier in the window. Items of one occurrence level have distinct
-    // destinations, so warps 0-2 apply level after level, every (item, element) update of a level in
-    // parallel; warp 3 meanwhile adds the (z,z) block's items one after another in queue order. So every
-    // element receives the reference's contributions in the reference's order. The column block
-    // accumulates in shared memory (in_smem, rows of 3 doubles) or in place in H.
+    // destinations, so every warp but the last applies level after level, every (item, element) update of
+    // a level in parallel; the last warp meanwhile adds the (z,z) block's items one after another in queue
+    // order. So every element receives the reference's contributions in the reference's order. The
+    // column block accumulates in shared memory (in_smem, rows of 3 doubles) or in place in H.
     __global__ void __launch_bounds__(COL_T)
         k_hess_col(TablesView tb, std::int64_t n, int const* __restrict__ cols, long long const* __restrict__ offs,
                    int const* __restrict__ idx, double const* __restrict__ dr, std::uint32_t const* __restrict__ types,
@@ -362,11 +363,11 @@ namespace flygpu {
               ++pos;
             }
           __syncthreads();
-          // values of the (g,z) items (warps 1-3, two items an iteration), and meanwhile the occurrence
+          // values of the (g,z) items (every warp but warp 0, two items an iteration), and meanwhile the occurrence
           // numbers (warp 0, in queue order)
           if (warp > 0)
-            for (int i0 = t - 32; i0 < nq; i0 += 192) {
-              int ii[2] = {i0, i0 + 96};
+            for (int i0 = t - 32; i0 < nq; i0 += 2 * COL_WORK) {
+              int ii[2] = {i0, i0 + COL_WORK};
               bool g2[2];
               long long q2[2];
               int j2[2];
@@ -465,10 +466,10 @@ namespace flygpu {
               S.lst[S.lvo[L] + atomicAdd(&S.lvc[L], 1)] = static_cast<short>(i);
             }
           __syncthreads();
-          if (warp < 3) {
+          if (warp < COL_T / 32 - 1) {
             for (int L = 0; L <= maxocc; ++L) {
               int const o0 = S.lvo[L], U = 9 * (S.lvo[L + 1] - o0);
-              for (int u = t; u < U; u += 96) {
+              for (int u = t; u < U; u += COL_WORK) {
                 int const i = S.lst[o0 + u / 9], e = u % 9;
                 double* const x = colp + (3 * static_cast<std::int64_t>(S.dest[i]) + e / 3) * cs + e % 3;
                 int const k2 = S.kind[i];
