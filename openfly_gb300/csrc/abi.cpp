@@ -138,11 +138,14 @@ namespace flygpu {
   // link while the kernel runs, instead of in a copy after it.
   double* device_alias(double* host) {
     cudaPointerAttributes pa{};
-    if (cudaPointerGetAttributes(&pa, host) != cudaSuccess) {
+    int dev = 0;
+    if (cudaPointerGetAttributes(&pa, host) != cudaSuccess || cudaGetDevice(&dev) != cudaSuccess) {
       cudaGetLastError();
       return nullptr;
     }
-    return pa.type == cudaMemoryTypeHost && pa.devicePointer ? static_cast<double*>(pa.devicePointer) : nullptr;
+    // host memory pinned under another device's context may not be mapped for this one: copy instead
+    bool const mapped_here = pa.type == cudaMemoryTypeHost && pa.devicePointer && pa.device == dev;
+    return mapped_here ? static_cast<double*>(pa.devicePointer) : nullptr;
   }
 
   void run_eam(flygpu_eam* E, flygpu_list* L, int precision, double* d_energy, double* d_grad) {
